@@ -1,0 +1,373 @@
+"""Benchmark of the GB300 DEM step: particle-steps/s on the batched-colonies
+workload (256 colonies, log-uniform 500..50 000 spheres, FP32 pair math),
+with the plain FP64 form on the same workload beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload colonies|sphere_fp32|sphere_plain|rod_trees]
+                  [--precision fp32f|fp64]
+
+`value`  device-resident throughput: K steps replayed from the captured step
+         graph, timed with CUDA events on the context's stream (inputs are
+         larger than L2, or L2 is flushed between steps for small workloads).
+`e2e`    the same metric through the C ABI with host buffers: every step
+         copies x, y, z, radius, cell_type in (bmxg_set_state) and x, y, z,
+         vel out (bmxg_get_state) from pinned host memory.
+`roofline` the force kernel (the dominant one) timed per launch with CUDA
+         events in profiling mode, against the algorithmic bytes per
+         particle-step (64 B for the FP32 sphere form, 80 B for FP64 spheres)
+         and the measured HBM copy bandwidth.
+`cpu_baseline` the oracle (plain-C restatement of the reference path,
+         OpenMP over particles) on the host cores on a bounded sample.
+Multi-GPU: replicas (each rank runs its own copy of the workload; no data-path
+collective).  --impl reference times the CPU restatement of the reference
+path on the host cores (the reference itself needs AMReX and MPI, absent).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DEM particle-steps/s on 1 GB300: FP64 plain vs FP32 batched @ rel force err≤1e-5"
+UNIT = "particle-steps/s"
+L2_BYTES = 129 * 2 ** 20
+ALG_BYTES = {("sphere", 1): 64, ("sphere", 0): 80, ("rod", 1): 188, ("rod", 0): 212}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="colonies",
+                    choices=["colonies", "sphere_fp32", "sphere_plain", "rod_trees"])
+    ap.add_argument("--precision", default=None, choices=[None, "fp32f", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def workload(name):
+    from boltzmannmfx_gb300 import configs
+    return {"colonies": configs.colonies, "sphere_fp32": configs.sphere_fp32,
+            "sphere_plain": configs.sphere_plain, "rod_trees": configs.rod_trees}[name]()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[2 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(key):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        v = d.get(key)
+        if isinstance(v, dict):
+            return v.get("bytes_per_launch")
+    return None
+
+
+def cpu_baseline(w, budget_s=12.0):
+    """Oracle (OpenMP over particles, all host threads) on a bounded sample of
+    the workload: whole colonies until ~budget_s of CPU work."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    nth = os.cpu_count() or 1
+    sizes = np.diff(w.offsets)
+    # one step on a first slice to calibrate
+    take = 1
+    while take < len(sizes) and sizes[:take].sum() < 100_000:
+        take += 1
+    P = w.particles.subset(0, int(w.offsets[take]))
+    t1 = O.time_evolve(w.params, w.geoms[:take], w.offsets[:take + 1], P, w.dt, 1, nth)
+    rate = sizes[:take].sum() / max(t1, 1e-9)
+    steps = int(max(1, min(w.steps, budget_s * rate / max(sizes[:take].sum(), 1))))
+    P = w.particles.subset(0, int(w.offsets[take]))
+    t = O.time_evolve(w.params, w.geoms[:take], w.offsets[:take + 1], P, w.dt, steps, nth)
+    n = int(sizes[:take].sum())
+    return {"value": n * steps / t, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{take} of {len(sizes)} colonies ({n} particles) x {steps} steps, FP64, "
+                      f"{t:.1f} s wall"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    from oracle import oracle as O
+    O.build(ref=False)
+    nth = os.cpu_count() or 1
+    sizes = np.diff(w.offsets)
+    take = 1
+    while take < len(sizes) and sizes[:take].sum() < 60_000:
+        take += 1
+    n = int(sizes[:take].sum())
+    P = w.particles.subset(0, int(w.offsets[take]))
+    g, off = w.geoms[:take], w.offsets[:take + 1]
+    O.time_evolve(w.params, g, off, P, w.dt, args.warmup, nth)
+    t = O.time_evolve(w.params, g, off, P, w.dt, args.steps, nth)
+    v = n * args.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic, seeded (BASELINE configuration distributions)",
+            "config": {"workload": w.name, "sample_particles": n, "sample_colonies": take},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"{take} colonies ({n} particles) per step, FP64, OpenMP"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference path (oracle/bmx_oracle.c); the reference "
+                    "itself needs AMReX and MPI, which are not available"}
+    print(json.dumps(line), flush=True)
+
+
+def pinned_particles(P, fields):
+    """Copy of the fields in page-locked host memory (numpy views of pinned torch tensors)."""
+    import torch
+    from boltzmannmfx_gb300.abi import Particles
+    Q = Particles.__new__(Particles)
+    Q.n, Q.rods, Q.a = P.n, P.rods, {}
+    keep = []
+    for k, v in P.a.items():
+        if k in fields:
+            t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                            pin_memory=True)
+            a = t.numpy()
+            a[...] = v
+            keep.append(t)
+            Q.a[k] = a
+        else:
+            Q.a[k] = v
+    Q._pinned = keep
+    return Q
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from boltzmannmfx_gb300 import Context, build
+    from boltzmannmfx_gb300.abi import BMXG_FP32F, BMXG_FP64
+    if rank == 0:
+        build.build()
+    if world > 1:
+        dist.barrier()
+    w = workload(args.workload)
+    prec = {"fp32f": BMXG_FP32F, "fp64": BMXG_FP64, None: w.precision}[args.precision]
+    kind = "rod" if w.particles.rods else "sphere"
+    N = w.n
+    stream = torch.cuda.Stream()
+    ctx = Context(w.params, w.geoms)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_state(w.particles, w.offsets)
+    ctx.autotune(os.path.join(ROOT, "boltzmannmfx_gb300", "_build", "autotune.json"))
+    ctx.set_state(w.particles, w.offsets)
+    state_bytes = N * (24 * 2 + 16 * 2 + 8 * 2 + 4 * 2 + 8 + 4 + 1 + 24)
+    flush = state_bytes < 2 * L2_BYTES
+    scratch = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda") if flush else None
+
+    def timed_steps(precision, K):
+        """K steps; device time in ms summed over CUDA-event brackets."""
+        if not flush:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            ctx.step(w.dt, K, precision)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            return e0.elapsed_time(e1)
+        tot = 0.0
+        for _ in range(K):
+            with torch.cuda.stream(stream):
+                scratch.add_(1.0)   # write a buffer larger than L2
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            ctx.step(w.dt, 1, precision)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot
+
+    # warm-up, then the timed K steps
+    timed_steps(prec, max(args.warmup, 3))
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.stats()["n_kernel_launches"]
+    with ClockSampler(local) as clk:
+        ms = timed_steps(prec, args.steps)
+    torch.cuda.synchronize()
+    launches = ctx.stats()["n_kernel_launches"] - l0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = N * world * args.steps / (ms / 1e3)
+
+    # roofline: the force kernel timed per launch (profiling mode, eager launches)
+    ctx.set_profiling(True)
+    kprof = min(args.steps, 40)
+    timed_steps(prec, kprof)
+    st = ctx.stats()
+    ctx.set_profiling(False)
+    k_ms = st["main_kernel_ms"] / max(st["main_kernel_launches"], 1)
+    alg = ALG_BYTES[(kind, 1 if prec == BMXG_FP32F else 0)] * N
+    peak, peak_kind = measured_peak()
+    achieved = alg / (k_ms / 1e3) / 1e9
+    kname = ("k_sphere" if kind == "sphere" else "k_rod_force") + ("<FP32F>" if prec == BMXG_FP32F else "<FP64>")
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "kernel_ms": k_ms,
+            "algorithmic_bytes_per_launch": alg,
+            "traffic": ncu_traffic(f"{w.name}:{kname}")}
+
+    # the other form on the same workload, and the FP32F force error against FP64
+    other = BMXG_FP64 if prec == BMXG_FP32F else BMXG_FP32F
+    ctx.set_state(w.particles, w.offsets)
+    timed_steps(other, 3)
+    ms_other = timed_steps(other, args.steps)
+    v_other = N * args.steps / (ms_other / 1e3)
+    fields = ("velx", "vely", "velz", "x")
+    ctx.set_state(w.particles, w.offsets)
+    ctx.step(w.dt, 1, BMXG_FP64)
+    A = w.particles.copy()
+    ctx.get_state(A, fields)
+    ctx.set_state(w.particles, w.offsets)
+    ctx.step(w.dt, 1, BMXG_FP32F)
+    B = w.particles.copy()
+    ctx.get_state(B, fields)
+    va = np.stack([A["velx"], A["vely"], A["velz"]])
+    vb = np.stack([B["velx"], B["vely"], B["velz"]])
+    rel_err = float(np.abs(va - vb).max() / np.abs(va).max())
+
+    # end to end through the C ABI with pinned host buffers
+    fin = ("x", "y", "z", "radius", "cell_type")
+    fout = ("x", "y", "z", "velx", "vely", "velz")
+    H = pinned_particles(w.particles, set(fin) | set(fout))
+    ke = min(args.steps, 20)
+    for _ in range(2):
+        ctx.set_state(H, w.offsets, fields=fin)
+        ctx.step(w.dt, 1, prec)
+        ctx.get_state(H, fout)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        ctx.set_state(H, w.offsets, fields=fin)
+        ctx.step(w.dt, 1, prec)
+        ctx.get_state(H, fout)
+    te = time.perf_counter() - t0
+    e2e = {"value": N * world * ke / te, "unit": UNIT,
+           "h2d_bytes_per_step": int(H.nbytes(fin)), "d2h_bytes_per_step": int(H.nbytes(fout)),
+           "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(w)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if prec == BMXG_FP32F else "f64",
+                "data": "synthetic, seeded (BASELINE configuration distributions)",
+                "config": {"workload": w.name, "particles": N, "colonies": w.ncol,
+                           "form": "FP32F" if prec == BMXG_FP32F else "FP64",
+                           "parallelism": f"replicas x{world}",
+                           "l2": ("L2 flushed between steps" if flush else
+                                  f"inputs larger than L2 (state {state_bytes / 2**20:.0f} MiB)")},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk.summary(),
+                "other_form": {"form": "FP64" if other == BMXG_FP64 else "FP32F", "value": v_other,
+                               "unit": UNIT, "ms_per_step": ms_other / args.steps},
+                "fp32f_over_fp64": (value / v_other) if prec == BMXG_FP32F else (v_other / value),
+                "rel_force_err_fp32f_vs_fp64": rel_err}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,846 @@
+// bmxg_ctx.cu -- host side of the C ABI (include/bmxg.h): context lifetime,
+// state upload / readback, the graph-captured step loop, neighbour-list
+// export, statistics and the launch-shape autotuner.
+//
+// Stands behind BMXParticleContainer::EvolveParticles
+// (src/des/bmx_pc.H:126-129, src/des/bmx_pc_interaction.cpp:13-495).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/bmxg.h"
+#include "bmxg_kernels.cuh"
+
+using namespace bmxg;
+
+namespace {
+
+struct GraphKey {
+    double dt;
+    int precision;
+    int parity;
+    bool operator<(const GraphKey &o) const
+    {
+        if (dt != o.dt) return dt < o.dt;
+        if (precision != o.precision) return precision < o.precision;
+        return parity < o.parity;
+    }
+};
+
+struct Shape {
+    int block = 256;
+    int grid = 0;  // 0: derive from occupancy
+};
+
+}  // namespace
+
+struct bmxg_ctx {
+    std::string err;
+    bmxg_params prm{};
+    int ncol = 0;
+    std::vector<bmxg_geometry> geoms;
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // device allocations
+    std::vector<void *> allocs;
+    DevState S{};
+    DevGeom *d_geoms = nullptr;
+    std::vector<DevGeom> h_geoms;
+    DevCounters *d_cnt = nullptr;
+    DevCounters *h_cnt = nullptr;  // pinned
+    int *scan_scratch = nullptr;
+    // staging in caller order
+    double *ud = nullptr;  // n doubles
+    int *ui = nullptr;     // 13 n ints
+    int *uperm = nullptr;
+
+    int64_t n = 0;
+    bool have_state = false;
+    bool stepped = false;
+    int parity = 0;
+    std::vector<int64_t> offsets;
+
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, int> graph_kernels;  // kernels per replay of each graph
+    Shape sh_sphere[2], sh_rod, sh_misc;
+    bmxg_stats stats{};
+    int64_t launches = 0;                   // kernels enqueued (graph nodes counted per replay)
+    bool profiling = false;
+    std::vector<cudaEvent_t> kev;           // event pairs around the force kernel, profiling mode
+    size_t kev_used = 0;
+};
+
+namespace {
+
+int fail(bmxg_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? BMXG_ERR_OOM : BMXG_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    } while (0)
+
+template <class T>
+int dalloc(bmxg_ctx *ctx, T **p, size_t count)
+{
+    void *q = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(&q, count * sizeof(T)));
+    ctx->allocs.push_back(q);
+    *p = (T *)q;
+    return BMXG_OK;
+}
+
+void drop_graphs(bmxg_ctx *ctx)
+{
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second);
+    ctx->graphs.clear();
+    ctx->graph_kernels.clear();
+}
+
+void free_state(bmxg_ctx *ctx)
+{
+    drop_graphs(ctx);
+    for (void *p : ctx->allocs) cudaFree(p);
+    ctx->allocs.clear();
+    ctx->S = DevState{};
+    ctx->d_geoms = nullptr;
+    ctx->scan_scratch = nullptr;
+    ctx->ud = nullptr;
+    ctx->ui = nullptr;
+    ctx->uperm = nullptr;
+    ctx->have_state = false;
+}
+
+int grid_for(bmxg_ctx *ctx, const Shape &s, int64_t n)
+{
+    int g = s.grid;
+    if (g <= 0) g = ctx->nsm * std::max(1, 2048 / s.block);
+    int64_t need = (n + s.block - 1) / s.block;
+    if (need < 1) need = 1;
+    return (int)std::min<int64_t>(g, need);
+}
+
+DevParams dev_params(const bmxg_params &p)
+{
+    return DevParams{p.bndry_width, p.stiffness,     p.z_wall,      p.z_bndry_width, p.z_stiffness,
+                     p.z_gravity,   p.bond_strength, p.bond_cutoff, p.viscosity,     p.neighborhood};
+}
+
+int check_params(const bmxg_params *p)
+{
+    if (!p) return BMXG_ERR_ARG;
+    const double v[10] = {p->bndry_width, p->stiffness,     p->z_wall,      p->z_bndry_width, p->z_stiffness,
+                          p->z_gravity,   p->bond_strength, p->bond_cutoff, p->viscosity,     p->neighborhood};
+    for (double x : v)
+        if (!std::isfinite(x)) return BMXG_ERR_ARG;
+    return BMXG_OK;
+}
+
+int check_geom(const bmxg_geometry &g, std::string &why)
+{
+    for (int d = 0; d < 3; ++d) {
+        if (!(g.prob_hi[d] > g.prob_lo[d]) || !std::isfinite(g.prob_lo[d]) || !std::isfinite(g.prob_hi[d])) {
+            why = "prob_hi must exceed prob_lo";
+            return BMXG_ERR_ARG;
+        }
+        if (g.n_cell[d] < 1 || g.n_cell[d] > (1 << 20)) {
+            why = "n_cell out of range";
+            return BMXG_ERR_ARG;
+        }
+        if (g.is_periodic[d] && g.n_cell[d] < 3) {
+            why = "a periodic direction needs n_cell >= 3";
+            return BMXG_ERR_UNSUPPORTED;
+        }
+    }
+    if (g.is_periodic[2]) {
+        why = "z must be non-periodic (the growth surface sits in z)";
+        return BMXG_ERR_UNSUPPORTED;
+    }
+    return BMXG_OK;
+}
+
+// Device geometry of each colony, with the column and slot numbering.
+void build_geoms(bmxg_ctx *ctx)
+{
+    ctx->h_geoms.resize(ctx->ncol);
+    int col_base = 0;
+    for (int c = 0; c < ctx->ncol; ++c) {
+        const bmxg_geometry &g = ctx->geoms[c];
+        DevGeom &G = ctx->h_geoms[c];
+        std::memset(&G, 0, sizeof(G));
+        double diag2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            G.plo[d] = g.prob_lo[d];
+            G.phi[d] = g.prob_hi[d];
+            G.len[d] = g.prob_hi[d] - g.prob_lo[d];
+            G.n[d] = g.n_cell[d];
+            G.dx[d] = G.len[d] / (double)G.n[d];
+            G.dxi[d] = 1.0 / G.dx[d];
+            G.dxf[d] = (float)G.dx[d];
+            G.per[d] = g.is_periodic[d] ? 1 : 0;
+            diag2 += 4.0 * G.dx[d] * G.dx[d];
+        }
+        G.col_base = col_base;
+        col_base += G.n[0] * G.n[1];
+        G.slot_base = (int)ctx->offsets[c];
+        G.slot_end = (int)ctx->offsets[c + 1];
+        // two bins apart at most per axis: |r|^2 < 4 (dx^2 + dy^2 + dz^2)
+        G.nbh_trivial = (ctx->prm.neighborhood >= diag2 * (1.0 + 1e-9)) ? 1 : 0;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmxg_version(void) { return BMXG_ABI_VERSION; }
+
+const char *bmxg_last_error(const bmxg_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bmxg_create(const bmxg_params *params, int32_t ncolonies, const bmxg_geometry *geoms, bmxg_ctx **out)
+{
+    if (!out) return BMXG_ERR_ARG;
+    *out = nullptr;
+    if (check_params(params) || ncolonies < 1 || !geoms) return BMXG_ERR_ARG;
+    bmxg_ctx *ctx = new bmxg_ctx();
+    ctx->prm = *params;
+    ctx->ncol = ncolonies;
+    ctx->geoms.assign(geoms, geoms + ncolonies);
+    for (int c = 0; c < ncolonies; ++c) {
+        std::string why;
+        int rc = check_geom(ctx->geoms[c], why);
+        if (rc) {
+            delete ctx;
+            return rc;
+        }
+    }
+    int64_t cols = 0;
+    for (auto &g : ctx->geoms) cols += (int64_t)g.n_cell[0] * g.n_cell[1];
+    if (cols >= (1LL << 31) - 2) {
+        delete ctx;
+        return BMXG_ERR_UNSUPPORTED;
+    }
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_cnt, sizeof(DevCounters));
+    if (e != cudaSuccess) {
+        ctx->err = cudaGetErrorString(e);
+        bmxg_destroy(ctx);
+        return BMXG_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    ctx->sh_sphere[0].block = 256;
+    ctx->sh_sphere[1].block = 256;
+    ctx->sh_rod.block = 128;
+    ctx->sh_misc.block = 256;
+    *out = ctx;
+    return BMXG_OK;
+}
+
+void bmxg_destroy(bmxg_ctx *ctx)
+{
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_state(ctx);
+    if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (check_params(params)) return fail(ctx, BMXG_ERR_ARG, "non-finite force parameter");
+    ctx->prm = *params;
+    drop_graphs(ctx);
+    if (ctx->have_state) {
+        build_geoms(ctx);
+        CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol,
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return BMXG_OK;
+}
+
+int bmxg_set_stream(bmxg_ctx *ctx, void *stream)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->own_stream;
+    if (s != ctx->stream) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->stream = s;
+        drop_graphs(ctx);
+    }
+    return BMXG_OK;
+}
+
+int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony_offsets, int where)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!p || p->n < 0 || !p->x || !p->y || !p->z || !p->radius || !p->cell_type)
+        return fail(ctx, BMXG_ERR_ARG, "x, y, z, radius and cell_type are required");
+    if (p->n > (1LL << 30)) return fail(ctx, BMXG_ERR_UNSUPPORTED, "more than 2^30 particles");
+    if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
+    const int64_t n = p->n;
+    std::vector<int64_t> off(ctx->ncol + 1, 0);
+    if (ctx->ncol == 1) {
+        off[1] = n;
+    } else {
+        if (!colony_offsets) return fail(ctx, BMXG_ERR_ARG, "colony_offsets required for several colonies");
+        for (int c = 0; c <= ctx->ncol; ++c) off[c] = colony_offsets[c];
+        if (off[0] != 0 || off[ctx->ncol] != n) return fail(ctx, BMXG_ERR_ARG, "colony_offsets must span 0..n");
+        for (int c = 0; c < ctx->ncol; ++c)
+            if (off[c + 1] < off[c]) return fail(ctx, BMXG_ERR_ARG, "colony_offsets must not decrease");
+    }
+    const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    // cell types decide which path runs; rods need their fields
+    std::vector<int32_t> ct((size_t)n);
+    if (n) {
+        if (where == BMXG_HOST) std::memcpy(ct.data(), p->cell_type, sizeof(int32_t) * n);
+        else CK(cudaMemcpy(ct.data(), p->cell_type, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    }
+    bool rods = false;
+    for (int64_t i = 0; i < n; ++i) {
+        if (ct[i] != BMXG_YEAST && ct[i] != BMXG_FUNGI) return fail(ctx, BMXG_ERR_ARG, "cell_type must be 0 or 1");
+        rods |= (ct[i] == BMXG_FUNGI);
+    }
+    if (rods && (!p->c_length || !p->theta || !p->phi || !p->area || !p->id || !p->cpu || !p->n_bnds ||
+                 !p->seg_id1 || !p->seg_id2 || !p->site))
+        return fail(ctx, BMXG_ERR_ARG, "rod segments need c_length, theta, phi, area, id, cpu and the bond table");
+
+    CK(cudaStreamSynchronize(ctx->stream));
+    // Same particle count, colony layout and cell-type mix as the loaded
+    // state: keep the device buffers (and the captured step graphs, which
+    // only hold their addresses) and overwrite the contents.
+    const bool reuse = ctx->have_state && ctx->n == n && ctx->offsets == off && ctx->S.has_rods == (rods ? 1 : 0);
+    if (!reuse) free_state(ctx);
+    ctx->n = n;
+    ctx->offsets = off;
+    build_geoms(ctx);
+    int64_t ncols = 0;
+    for (auto &g : ctx->geoms) ncols += (int64_t)g.n_cell[0] * g.n_cell[1];
+
+    DevState &S = ctx->S;
+    S.n = (int)n;
+    S.ncol = ctx->ncol;
+    S.ncols_total = (int)ncols;
+    S.has_rods = rods ? 1 : 0;
+    int rc = BMXG_OK;
+#define AL(ptr, cnt)                       \
+    do {                                   \
+        rc = dalloc(ctx, &(ptr), (cnt));   \
+        if (rc) return rc;                 \
+    } while (0)
+    if (!reuse) {
+    AL(ctx->d_geoms, ctx->ncol);
+    AL(ctx->d_cnt, 1);
+    for (int k = 0; k < 2; ++k) {
+        AL(S.x[k], n); AL(S.y[k], n); AL(S.z[k], n);
+        AL(S.rel[k], n); AL(S.col[k], n); AL(S.iz[k], n);
+        AL(S.perm[k], n); AL(S.colstart[k], ncols + 1);
+    }
+    AL(S.colcnt, ncols); AL(S.tmp, n);
+    AL(S.rad, n); AL(S.orig, n); AL(S.ctype, n);
+    AL(S.vx, n); AL(S.vy, n); AL(S.vz, n); AL(S.wx, n); AL(S.wy, n); AL(S.wz, n);
+    AL(ctx->scan_scratch, scan_scratch_ints((int)ncols));
+    AL(ctx->ud, n); AL(ctx->ui, 13 * n + 1); AL(ctx->uperm, n);
+    if (rods) {
+        AL(S.clen, n); AL(S.area, n); AL(S.bscale, n);
+        for (int k = 0; k < 2; ++k) { AL(S.theta[k], n); AL(S.phi[k], n); AL(S.trig[k], n); AL(S.tab[k], 13 * n); }
+        AL(S.id, n); AL(S.cpu, n); AL(S.fuse_tip, n); AL(S.position, n); AL(S.fix_site, n);
+        AL(S.fflag, n); AL(S.sflag, n); AL(S.nflag, n); AL(S.dltd, 6 * n); AL(S.fc, 6 * n);
+    }
+    }  // !reuse
+#undef AL
+    S.geoms = ctx->d_geoms;
+    S.cnt = ctx->d_cnt;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
+    CK(cudaMemsetAsync(S.colcnt, 0, sizeof(int) * std::max<int64_t>(ncols, 1), st));
+    if (n == 0) {
+        CK(cudaMemsetAsync(S.colstart[0], 0, sizeof(int) * (ncols + 1), st));
+        CK(cudaMemsetAsync(S.colstart[1], 0, sizeof(int) * (ncols + 1), st));
+        CK(cudaStreamSynchronize(st));
+        ctx->have_state = true;
+        ctx->parity = 0;
+        return BMXG_OK;
+    }
+    const int blk = ctx->sh_misc.block;
+    const int grd = grid_for(ctx, ctx->sh_misc, n);
+    // caller-order positions into the slot x/y/z of buffer 1 (scratch for now)
+    CK(cudaMemcpyAsync(S.x[1], p->x, sizeof(double) * n, kind, st));
+    CK(cudaMemcpyAsync(S.y[1], p->y, sizeof(double) * n, kind, st));
+    CK(cudaMemcpyAsync(S.z[1], p->z, sizeof(double) * n, kind, st));
+    // canonical order of the caller's particles
+    ctx->launches += launch_user_bin(S, S.x[1], S.y[1], S.z[1], S.col[1], S.iz[1], grd, blk, st);
+    ctx->launches += launch_scan(S.colcnt, S.colstart[1], (int)ncols, ctx->scan_scratch, st);
+    ctx->launches += launch_user_scatter_canon(S, S.col[1], S.iz[1], S.colstart[1], ctx->uperm, grd, blk, st);
+    CK(cudaMemcpyAsync(S.orig, ctx->uperm, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    // gather every field into slot order
+    ctx->launches += launch_gather_d(S.x[0], S.x[1], ctx->uperm, (int)n, grd, blk, st);
+    ctx->launches += launch_gather_d(S.y[0], S.y[1], ctx->uperm, (int)n, grd, blk, st);
+    ctx->launches += launch_gather_d(S.z[0], S.z[1], ctx->uperm, (int)n, grd, blk, st);
+    auto up_d = [&](const double *src, double *dst, double fill) -> int {
+        if (src) {
+            CK(cudaMemcpyAsync(ctx->ud, src, sizeof(double) * n, kind, st));
+            ctx->launches += launch_gather_d(dst, ctx->ud, ctx->uperm, (int)n, grd, blk, st);
+        } else if (fill == 0.0) {
+            CK(cudaMemsetAsync(dst, 0, sizeof(double) * n, st));
+        } else {
+            std::vector<double> h((size_t)n, fill);
+            CK(cudaMemcpyAsync(ctx->ud, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
+            CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        }
+        return BMXG_OK;
+    };
+    auto up_i = [&](const int32_t *src, int *dst, int planes, int fill) -> int {
+        if (src) {
+            CK(cudaMemcpyAsync(ctx->ui, src, sizeof(int) * n * planes, kind, st));
+            ctx->launches += launch_gather_i(dst, ctx->ui, ctx->uperm, (int)n, planes, grd, blk, st);
+        } else {
+            CK(cudaMemsetAsync(dst, fill == 0 ? 0 : 0xff, sizeof(int) * n * planes, st));
+        }
+        return BMXG_OK;
+    };
+    if ((rc = up_d(p->radius, S.rad, 0.0))) return rc;
+    CK(cudaMemcpyAsync(ctx->ui, p->cell_type, sizeof(int) * n, kind, st));
+    ctx->launches += launch_gather_i8(S.ctype, ctx->ui, ctx->uperm, (int)n, grd, blk, st);
+    if ((rc = up_d(p->velx, S.vx, 0.0))) return rc;
+    if ((rc = up_d(p->vely, S.vy, 0.0))) return rc;
+    if ((rc = up_d(p->velz, S.vz, 0.0))) return rc;
+    if ((rc = up_d(p->wx, S.wx, 0.0))) return rc;
+    if ((rc = up_d(p->wy, S.wy, 0.0))) return rc;
+    if ((rc = up_d(p->wz, S.wz, 0.0))) return rc;
+    if (rods) {
+        if ((rc = up_d(p->c_length, S.clen, 0.0))) return rc;
+        if ((rc = up_d(p->area, S.area, 0.0))) return rc;
+        if ((rc = up_d(p->bond_scale, S.bscale, 1.0))) return rc;
+        if ((rc = up_d(p->theta, S.theta[0], 0.0))) return rc;
+        if ((rc = up_d(p->phi, S.phi[0], 0.0))) return rc;
+        if ((rc = up_i(p->id, S.id, 1, 0))) return rc;
+        if ((rc = up_i(p->cpu, S.cpu, 1, 0))) return rc;
+        if ((rc = up_i(p->fuse_tip, S.fuse_tip, 1, 0))) return rc;
+        if ((rc = up_i(p->position, S.position, 1, 0))) return rc;
+        if ((rc = up_i(p->fix_site, S.fix_site, 1, 0))) return rc;
+        if ((rc = up_i(p->fuse_flag, S.fflag, 1, 0))) return rc;
+        if ((rc = up_i(p->split_flag, S.sflag, 1, 0))) return rc;
+        if ((rc = up_i(p->new_flag, S.nflag, 1, 0))) return rc;
+        if ((rc = up_i(p->dltd, S.dltd, 6, -1))) return rc;
+        // bond table planes: n_bnds, ids[4], cpus[4], sites[4]
+        if ((rc = up_i(p->n_bnds, S.tab[0], 1, 0))) return rc;
+        if ((rc = up_i(p->seg_id1, S.tab[0] + n, 4, 0))) return rc;
+        if ((rc = up_i(p->seg_id2, S.tab[0] + 5 * n, 4, 0))) return rc;
+        if ((rc = up_i(p->site, S.tab[0] + 9 * n, 4, 0))) return rc;
+        ctx->launches += launch_trig(S, 0, grd, blk, st);
+    }
+    // bins of the slots and the first column lists
+    CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
+    ctx->launches += launch_bin(S, 0, grd, blk, st);
+    ctx->launches += launch_rebuild(S, 0, ctx->scan_scratch, grd, blk, st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    ctx->have_state = true;
+    ctx->stepped = false;
+    ctx->parity = 0;
+    std::memset(&ctx->stats, 0, sizeof(ctx->stats));
+    ctx->stats.n_particles = n;
+    return BMXG_OK;
+}
+
+int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (!p || p->n != ctx->n) return fail(ctx, BMXG_ERR_ARG, "particle count differs from the loaded state");
+    if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
+    const int64_t n = ctx->n;
+    if (n == 0) return BMXG_OK;
+    const DevState &S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    const int blk = ctx->sh_misc.block;
+    const int grd = grid_for(ctx, ctx->sh_misc, n);
+    const int a = ctx->parity;
+    auto out_d = [&](double *dst, const double *src) -> int {
+        if (!dst || !src) return BMXG_OK;
+        ctx->launches += launch_scatter_d(ctx->ud, src, S.orig, (int)n, grd, blk, st);
+        CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
+        CK(cudaStreamSynchronize(st));
+        return BMXG_OK;
+    };
+    auto out_i = [&](int32_t *dst, const int *src, int planes) -> int {
+        if (!dst || !src) return BMXG_OK;
+        ctx->launches += launch_scatter_i(ctx->ui, src, S.orig, (int)n, planes, grd, blk, st);
+        CK(cudaMemcpyAsync(dst, ctx->ui, sizeof(int) * n * planes, kind, st));
+        CK(cudaStreamSynchronize(st));
+        return BMXG_OK;
+    };
+    int rc;
+    if ((rc = out_d(p->x, S.x[a]))) return rc;
+    if ((rc = out_d(p->y, S.y[a]))) return rc;
+    if ((rc = out_d(p->z, S.z[a]))) return rc;
+    if ((rc = out_d(p->velx, S.vx))) return rc;
+    if ((rc = out_d(p->vely, S.vy))) return rc;
+    if ((rc = out_d(p->velz, S.vz))) return rc;
+    if ((rc = out_d(p->wx, S.wx))) return rc;
+    if ((rc = out_d(p->wy, S.wy))) return rc;
+    if ((rc = out_d(p->wz, S.wz))) return rc;
+    if (S.has_rods) {
+        if ((rc = out_d(p->theta, S.theta[a]))) return rc;
+        if ((rc = out_d(p->phi, S.phi[a]))) return rc;
+        if ((rc = out_i(p->n_bnds, S.tab[a], 1))) return rc;
+        if ((rc = out_i(p->seg_id1, S.tab[a] + n, 4))) return rc;
+        if ((rc = out_i(p->seg_id2, S.tab[a] + 5 * n, 4))) return rc;
+        if ((rc = out_i(p->site, S.tab[a] + 9 * n, 4))) return rc;
+        if ((rc = out_i(p->position, S.position, 1))) return rc;
+        if ((rc = out_i(p->fix_site, S.fix_site, 1))) return rc;
+        if ((rc = out_i(p->fuse_flag, S.fflag, 1))) return rc;
+        if ((rc = out_i(p->split_flag, S.sflag, 1))) return rc;
+        if ((rc = out_i(p->new_flag, S.nflag, 1))) return rc;
+        if ((rc = out_i(p->dltd, S.dltd, 6))) return rc;
+    } else if (ctx->stepped && where == BMXG_HOST) {
+        // spheres: the step only clears the fusion flags (bmx_pc_interaction.cpp:178-180)
+        for (int32_t *f : {p->fuse_flag, p->split_flag, p->new_flag})
+            if (f) std::memset(f, 0, sizeof(int32_t) * n);
+    } else if (ctx->stepped) {
+        for (int32_t *f : {p->fuse_flag, p->split_flag, p->new_flag})
+            if (f) CK(cudaMemsetAsync(f, 0, sizeof(int32_t) * n, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return BMXG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Enqueue one DEM step reading buffer a.
+void enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
+{
+    const DevState &S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    const DevParams P = dev_params(ctx->prm);
+    const int b = a ^ 1;
+    // per-step counters (out-of-domain, images, pairs, repairs); `nonfinite` is sticky
+    cudaMemsetAsync(ctx->d_cnt, 0, offsetof(DevCounters, nonfinite), st);
+    cudaMemsetAsync(&ctx->d_cnt->pairs, 0, sizeof(DevCounters) - offsetof(DevCounters, pairs), st);
+    const int64_t n = ctx->n;
+    const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
+    // profiling mode: an event pair around the force kernel of this step
+    cudaEvent_t k0 = nullptr, k1 = nullptr;
+    if (ctx->profiling) {
+        while (ctx->kev.size() < 2 * (ctx->kev_used + 1)) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) break;
+            ctx->kev.push_back(e);
+        }
+        if (ctx->kev.size() >= 2 * (ctx->kev_used + 1)) {
+            k0 = ctx->kev[2 * ctx->kev_used];
+            k1 = ctx->kev[2 * ctx->kev_used + 1];
+            ++ctx->kev_used;
+        }
+    }
+    if (!S.has_rods) {
+        const Shape &sh = ctx->sh_sphere[precision == BMXG_FP32F ? 1 : 0];
+        if (k0) cudaEventRecord(k0, st);
+        ctx->launches += launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st);
+        if (k1) cudaEventRecord(k1, st);
+    } else {
+        const int rg = grid_for(ctx, ctx->sh_rod, n);
+        ctx->launches += launch_rod_book(S, P, a, rg, ctx->sh_rod.block, st);
+        if (k0) cudaEventRecord(k0, st);
+        ctx->launches += launch_rod_force(S, P, a, precision, rg, ctx->sh_rod.block, st);
+        if (k1) cudaEventRecord(k1, st);
+        ctx->launches += launch_rod_update(S, dt, a, mgrd, mblk, st);
+    }
+    ctx->launches += launch_rebuild(S, b, ctx->scan_scratch, mgrd, mblk, st);
+}
+
+int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec_t *out)
+{
+    GraphKey key{dt, precision, parity};
+    auto it = ctx->graphs.find(key);
+    if (it != ctx->graphs.end()) {
+        *out = it->second;
+        return BMXG_OK;
+    }
+    cudaGraph_t g = nullptr;
+    const int64_t before = ctx->launches;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(ctx, dt, precision, parity);
+    enqueue_step(ctx, dt, precision, parity ^ 1);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->graph_kernels[key] = (int)(ctx->launches - before);  // counted per replay instead
+    ctx->launches = before;
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    ctx->graphs[key] = ex;
+    *out = ex;
+    return BMXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt or nsteps");
+    if (precision != BMXG_FP64 && precision != BMXG_FP32F) return fail(ctx, BMXG_ERR_ARG, "bad precision");
+    if (ctx->n == 0 || nsteps == 0) return BMXG_OK;
+    // nsubsteps = ceil(dt / dtsolid) with dtsolid := dt, subdt = dt / nsubsteps
+    // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
+    const double subdt = dt / 1.0;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    int32_t left = nsteps;
+    ctx->kev_used = 0;
+    if (left >= 2 && !ctx->profiling) {
+        cudaGraphExec_t g = nullptr;
+        int rc = get_graph(ctx, subdt, precision, ctx->parity, &g);
+        if (rc) return rc;
+        const int per = ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity}];
+        while (left >= 2) {
+            CK(cudaGraphLaunch(g, ctx->stream));
+            ctx->launches += per;
+            left -= 2;
+        }
+    }
+    while (left >= 1) {  // odd remainder, or every step in profiling mode
+        enqueue_step(ctx, subdt, precision, ctx->parity);
+        ctx->parity ^= 1;
+        --left;
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stepped = true;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.last_step_ms = ms;
+    for (size_t k = 0; k < ctx->kev_used; ++k) {
+        float km = 0.0f;
+        if (cudaEventElapsedTime(&km, ctx->kev[2 * k], ctx->kev[2 * k + 1]) == cudaSuccess) {
+            ctx->stats.main_kernel_ms += km;
+            ctx->stats.main_kernel_launches += 1;
+        }
+    }
+    ctx->kev_used = 0;
+    ctx->stats.n_kernel_launches = ctx->launches;
+    ctx->stats.n_out_of_domain = (int64_t)ctx->h_cnt->out_of_domain;
+    ctx->stats.n_edge_ghost = (int64_t)ctx->h_cnt->edge_ghost;
+    ctx->stats.n_bond_repairs = (int64_t)ctx->h_cnt->bond_repairs;
+    ctx->stats.n_rebins += nsteps;
+    if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
+    return BMXG_OK;
+}
+
+int bmxg_evolve_particles(bmxg_ctx *ctx, double dt, double *cost_per_colony, int32_t *nsubsteps)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    int rc = bmxg_step(ctx, dt, 1, BMXG_FP64);
+    if (rc) return rc;
+    if (nsubsteps) *nsubsteps = 1;
+    if (cost_per_colony)  // "NumParticles" knapsack weight (bmx_pc_interaction.cpp:470-473)
+        for (int c = 0; c < ctx->ncol; ++c) cost_per_colony[c] = (double)(ctx->offsets[c + 1] - ctx->offsets[c]);
+    return BMXG_OK;
+}
+
+int bmxg_get_stats(const bmxg_ctx *ctx, bmxg_stats *out)
+{
+    if (!ctx || !out) return BMXG_ERR_ARG;
+    *out = ctx->stats;
+    out->n_kernel_launches = ctx->launches;
+    return BMXG_OK;
+}
+
+int bmxg_set_profiling(bmxg_ctx *ctx, int32_t on)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    ctx->profiling = on != 0;
+    if (ctx->profiling) {
+        ctx->stats.main_kernel_ms = 0.0;
+        ctx->stats.main_kernel_launches = 0;
+    }
+    return BMXG_OK;
+}
+
+int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int64_t cap, int64_t *total)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (!offs || !total) return fail(ctx, BMXG_ERR_ARG, "offs and total are required");
+    const int64_t n = ctx->n;
+    offs[0] = 0;
+    *total = 0;
+    if (n == 0) return BMXG_OK;
+    cudaStream_t st = ctx->stream;
+    const DevParams P = dev_params(ctx->prm);
+    int64_t *d_offs = nullptr;
+    CK(cudaMallocAsync((void **)&d_offs, sizeof(int64_t) * (n + 1), st));
+    const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, n);
+    ctx->launches += launch_pairs(ctx->S, P, ctx->parity, d_offs, nullptr, nullptr, 0, grd, blk, st);
+    std::vector<int64_t> cnt((size_t)n);
+    cudaError_t e = cudaMemcpyAsync(cnt.data(), d_offs, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(d_offs, st);
+        return fail(ctx, BMXG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (int64_t i = 0; i < n; ++i) offs[i + 1] = offs[i] + cnt[(size_t)i];
+    *total = offs[n];
+    ctx->stats.n_pairs_last = offs[n];
+    if (offs[n] > cap || !idx || !img) {
+        cudaFreeAsync(d_offs, st);
+        cudaStreamSynchronize(st);
+        return (offs[n] > cap) ? fail(ctx, BMXG_ERR_CAPACITY, "pair buffer too small") : BMXG_OK;
+    }
+    int *d_idx = nullptr;
+    int8_t *d_img = nullptr;
+    const int64_t m = std::max<int64_t>(offs[n], 1);
+    e = cudaMallocAsync((void **)&d_idx, sizeof(int) * m, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_img, m, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_offs, offs, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        ctx->launches += launch_pairs(ctx->S, P, ctx->parity, d_offs, d_idx, d_img, 1, grd, blk, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(idx, d_idx, sizeof(int) * offs[n], cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(img, d_img, offs[n], cudaMemcpyDeviceToHost, st);
+    if (d_idx) cudaFreeAsync(d_idx, st);
+    if (d_img) cudaFreeAsync(d_img, st);
+    cudaFreeAsync(d_offs, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, cudaGetErrorString(e));
+    return BMXG_OK;
+}
+
+int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (ctx->n == 0 || ctx->S.has_rods) return BMXG_OK;
+    const int64_t n = ctx->n;
+    char devname[256] = {0};
+    {
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, ctx->device));
+        std::snprintf(devname, sizeof(devname), "%s", prop.name);
+    }
+    char key[512];
+    // look the shape up in the cache
+    for (int prec = 0; prec < 2; ++prec) {
+        std::snprintf(key, sizeof(key), "\"%s|sphere|%d|n=%lld|ncol=%d\"", devname, prec, (long long)n, ctx->ncol);
+        bool hit = false;
+        if (cache_path) {
+            FILE *f = std::fopen(cache_path, "r");
+            if (f) {
+                std::string txt;
+                char buf[4096];
+                size_t r;
+                while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, r);
+                std::fclose(f);
+                size_t pos = txt.find(key);
+                int bb = 0, gg = 0;
+                if (pos != std::string::npos &&
+                    std::sscanf(txt.c_str() + pos + std::strlen(key), ": {\"block\": %d, \"grid\": %d}", &bb, &gg) == 2 &&
+                    bb > 0) {
+                    ctx->sh_sphere[prec].block = bb;
+                    ctx->sh_sphere[prec].grid = gg;
+                    hit = true;
+                }
+            }
+        }
+        if (hit) continue;
+        // sweep: the kernel reads buffer a and writes buffer b, so repeated
+        // launches leave the state as it was except for the column counters,
+        // which are cleared afterwards
+        const DevState &S = ctx->S;
+        const DevParams P = dev_params(ctx->prm);
+        float best = 1e30f;
+        Shape bs = ctx->sh_sphere[prec];
+        const int blocks[] = {64, 128, 256, 512};
+        for (int blk : blocks) {
+            for (int mult = 1; mult <= 16; mult *= 2) {
+                Shape s;
+                s.block = blk;
+                s.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
+                const int grd = grid_for(ctx, s, n);
+                for (int w = 0; w < 2; ++w)
+                    ctx->launches += launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream);
+                CK(cudaEventRecord(ctx->ev0, ctx->stream));
+                for (int r = 0; r < 5; ++r)
+                    ctx->launches += launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream);
+                CK(cudaEventRecord(ctx->ev1, ctx->stream));
+                CK(cudaEventSynchronize(ctx->ev1));
+                float ms = 0.0f;
+                CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                if (ms < best) {
+                    best = ms;
+                    bs = s;
+                }
+            }
+        }
+        CK(cudaMemsetAsync(ctx->S.colcnt, 0, sizeof(int) * std::max(ctx->S.ncols_total, 1), ctx->stream));
+        CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->sh_sphere[prec] = bs;
+        if (cache_path) {
+            std::string txt;
+            FILE *f = std::fopen(cache_path, "r");
+            if (f) {
+                char buf[4096];
+                size_t r;
+                while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, r);
+                std::fclose(f);
+            }
+            size_t close = txt.rfind('}');
+            char entry[768];
+            std::snprintf(entry, sizeof(entry), "%s: {\"block\": %d, \"grid\": %d, \"ms_per_5\": %.4f}", key,
+                          bs.block, bs.grid, best);
+            if (close == std::string::npos || txt.find('"') == std::string::npos)
+                txt = std::string("{\n  ") + entry + "\n}\n";
+            else
+                txt = txt.substr(0, close) + ",\n  " + entry + "\n}\n";
+            f = std::fopen(cache_path, "w");
+            if (f) {
+                std::fwrite(txt.data(), 1, txt.size(), f);
+                std::fclose(f);
+            }
+        }
+    }
+    drop_graphs(ctx);
+    return BMXG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// bmxg_dev.cuh -- device-side data layout and helpers of the DEM step.
+//
+// Layout in HBM (all structure-of-arrays, one entry per particle "slot").
+// Slots are the particles sorted once, at bmxg_set_state, by the canonical
+// neighbour-list key (colony, column, z-bin, original index); that order is
+// kept for the lifetime of the state, so neighbours that the stencil visits
+// sit close together in memory.  What changes every step is
+//   - positions x/y/z (FP64, ping-pong A/B),
+//   - the packed bin of each slot (column id + z bin, ping-pong),
+//   - the per-column start offsets and the column-sorted slot list `perm`
+//     (ping-pong), rebuilt by a counting sort every step exactly as the
+//     reference rebuilds its neighbour list every step
+//     (src/des/bmx_pc_interaction.cpp:97-103).
+// A "column" is the (x-bin, y-bin) pair of one colony; a column holds its
+// particles sorted by (z-bin, original index), so the three z-bins of a
+// stencil row are one contiguous run -- the order in which AMReX's
+// NeighborList walks its 27 bins (x outermost, z innermost, ascending index
+// within a bin).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bmxg {
+
+constexpr double kPi = 3.14159265358979323846;  // M_PI as the reference uses it
+constexpr double kSmall = 1.0e-15;              // small_number, bmx_pc_interaction.cpp:157
+constexpr int BMXG_FP64_FORM = 0;               // BMXG_FP64 of bmxg.h
+constexpr int BMXG_FP32F_FORM = 1;              // BMXG_FP32F of bmxg.h
+constexpr int kYeast = 0, kFungi = 1;           // cellType (src/chemistry/bmx_chem.H:120-126)
+constexpr int kTip = 0, kSecond1 = 1, kSecond2 = 2, kInterior = 3;  // siteLocation (bmx_chem.H:128-136)
+
+// Geometry of one colony (an AMReX level geometry) plus its place in the
+// global column / slot numbering.
+struct DevGeom {
+    double plo[3], phi[3], len[3], dx[3], dxi[3];
+    float dxf[3];
+    int n[3];
+    int per[3];
+    int col_base;       // first global column of this colony
+    int slot_base;      // first slot of this colony
+    int slot_end;       // one past the last slot
+    int nbh_trivial;    // 1: BMXCheckPair's r^2 <= neighborhood holds for every stencil pair
+};
+
+// Counters a step accumulates on the device.
+struct DevCounters {
+    unsigned long long out_of_domain;
+    unsigned long long edge_ghost;
+    unsigned long long nonfinite;
+    unsigned long long pairs;
+    unsigned long long bond_repairs;
+    unsigned long long moved;
+};
+
+// Force parameters, fpar[0..8] (src/chemistry/bmx_cell_interaction.cpp:84-93).
+struct DevParams {
+    double bw, k, z_wall, z_bw, z_k, z_g, k_bond, bond_cutoff, visc, nbh;
+};
+
+// Bin index along one axis in the coordinates of the box grown by one cell:
+// (int)((x - plo)*dxi - lo) with lo = -1, as AMReX's NeighborList bins.
+// Explicit round-to-nearest intrinsics keep it free of FMA contraction so
+// the bins are bit-identical to the host oracle's.  Clamped to [lo_c, hi_c].
+__device__ __forceinline__ int bin_of(double x, double plo, double dxi, int lo_c, int hi_c)
+{
+    double v = __dadd_rn(__dmul_rn(__dsub_rn(x, plo), dxi), 1.0);
+    if (!(v > (double)lo_c)) return lo_c;
+    if (v >= (double)hi_c + 1.0) return hi_c;
+    return (int)v;
+}
+
+// AMReX enforcePeriodic restated: shift by the domain length until inside,
+// then clamp against round-off.  Loops are bounded (a finite x leaves the
+// loop after |x|/len + 1 iterations; a non-finite x is caught by the caller).
+__device__ __forceinline__ double wrap1(double x, double lo, double hi, double len)
+{
+    if (x > hi) {
+        for (int it = 0; x > hi && it < 64; ++it) x = __dsub_rn(x, len);
+        if (x < lo) x = lo;
+    } else if (x < lo) {
+        for (int it = 0; x < lo && it < 64; ++it) x = __dadd_rn(x, len);
+        if (x > hi) x = hi;
+    }
+    return x;
+}
+
+__device__ __forceinline__ int colony_of(const DevGeom *geoms, int ncol, int slot)
+{
+    if (ncol == 1) return 0;
+    int lo = 0, hi = ncol - 1;
+    while (lo < hi) {  // last colony whose slot_base <= slot
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&geoms[mid].slot_base) <= slot) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Global column id of grown-box bin coordinates (bx, by) in 1..n.
+__device__ __forceinline__ int column_of(const DevGeom &g, int bx, int by)
+{
+    return g.col_base + (bx - 1) * g.n[1] + (by - 1);
+}
+
+// One stencil row (ii, jj) of a particle in grown bin (bx, by): the source
+// column whose particles (or their periodic images) fill that row, and the
+// image shift.  Returns false when the row lies outside a non-periodic face.
+__device__ __forceinline__ bool stencil_row(const DevGeom &g, int ii, int jj, int &col, int &sx, int &sy)
+{
+    int srcx = ii, srcy = jj;
+    sx = 0;
+    sy = 0;
+    if (ii == 0) { if (!g.per[0]) return false; srcx = g.n[0]; sx = -1; }
+    else if (ii == g.n[0] + 1) { if (!g.per[0]) return false; srcx = 1; sx = 1; }
+    if (jj == 0) { if (!g.per[1]) return false; srcy = g.n[1]; sy = -1; }
+    else if (jj == g.n[1] + 1) { if (!g.per[1]) return false; srcy = 1; sy = 1; }
+    col = column_of(g, srcx, srcy);
+    return true;
+}
+
+// Pack (z-bin, original index) into the 64-bit key that orders a column.
+__device__ __forceinline__ unsigned long long col_key(int iz, int orig)
+{
+    return ((unsigned long long)(unsigned)iz << 32) | (unsigned)orig;
+}
+
+}  // namespace bmxg

@@ -1,0 +1,82 @@
+// bmxg_kernels.cuh -- device state of a context and the host launchers of
+// every kernel (internal to libbmxg; the public surface is include/bmxg.h).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bmxg_dev.cuh"
+
+namespace bmxg {
+
+// Device pointers of one context.  [2] arrays are ping-pong buffers indexed
+// by the step parity a (read) / b = a ^ 1 (write).
+struct DevState {
+    int n;             // particles (slots)
+    int ncol;          // colonies
+    int ncols_total;   // columns over all colonies
+    const DevGeom *geoms;
+    DevCounters *cnt;
+
+    double *x[2], *y[2], *z[2];
+    float4 *rel[2];    // FP32 offsets from the slot's bin corner (x, y, z) + radius (w)
+    int *col[2];       // global column of the slot
+    int *iz[2];        // z bin (grown-box coordinates, 1..nz)
+    int *perm[2];      // slots sorted by (column, z bin, original index)
+    int *colstart[2];  // ncols_total + 1 offsets into perm
+    int *colcnt;       // per-column counter, zero between uses
+    int *tmp;          // scatter scratch, n entries
+
+    double *rad;
+    int *orig;         // slot -> caller's index
+    int8_t *ctype;     // cell_type
+
+    double *vx, *vy, *vz, *wx, *wy, *wz;  // step outputs (slot order)
+
+    // rod segments (null when the state holds spheres only)
+    int has_rods;
+    double *clen, *area, *bscale;
+    double *theta[2], *phi[2];
+    double4 *trig[2];  // (cos theta, sin theta, cos phi, sin phi)
+    int *id, *cpu, *fuse_tip;
+    int *tab[2];       // 13 planes: n_bnds, ids[4], cpus[4], sites[4]
+    int *position, *fix_site, *fflag, *sflag, *nflag;
+    int *dltd;         // 6 planes
+    double *fc;        // 6 planes, force gather of the rod path
+};
+
+// ---- binning / counting sort (k_bin.cu) ----------------------------------
+int launch_bin(const DevState &S, int b, int grid, int block, cudaStream_t st);
+int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st);
+size_t scan_scratch_ints(int n);
+int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st);
+int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st);
+
+// caller-order staging -> slot order (set_state) and back (get_state)
+int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz,
+                     int *ucol, int *uiz, int grid, int block, cudaStream_t st);
+int launch_user_scatter_canon(const DevState &S, const int *ucol, const int *uiz, const int *colstart,
+                               int *uperm, int grid, int block, cudaStream_t st);
+int launch_gather_d(double *dst, const double *src, const int *perm, int n, int grid, int block, cudaStream_t st);
+int launch_gather_i(int *dst, const int *src, const int *perm, int n, int planes, int grid, int block, cudaStream_t st);
+int launch_gather_i8(int8_t *dst, const int *src, const int *perm, int n, int grid, int block, cudaStream_t st);
+int launch_scatter_d(double *dst, const double *src, const int *orig, int n, int grid, int block, cudaStream_t st);
+int launch_scatter_i(int *dst, const int *src, const int *orig, int n, int planes, int grid, int block, cudaStream_t st);
+int launch_trig(const DevState &S, int b, int grid, int block, cudaStream_t st);
+
+// neighbour-list export (k_bin.cu): mode 0 counts per caller index, mode 1 fills
+int launch_pairs(const DevState &S, const DevParams &P, int a, int64_t *cnt_or_offs, int *idx,
+                  int8_t *img, int mode, int grid, int block, cudaStream_t st);
+
+// ---- spheres (k_sphere.cu) -----------------------------------------------
+// force gather + wall + update + rebin of every slot, reading buffer a and
+// writing buffer b; precision BMXG_FP64 / BMXG_FP32F
+int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision,
+                        int grid, int block, cudaStream_t st);
+
+// ---- rods and mixed states (k_rod.cu) ------------------------------------
+int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st);
+int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
+                      cudaStream_t st);
+int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st);
+
+}  // namespace bmxg

@@ -1,0 +1,115 @@
+// bmxg_stencil.cuh -- the neighbour traversal every kernel shares, and the
+// per-slot rebin.  Translation units that include this are compiled with
+// -fmad=false so that every FP64 expression rounds exactly like the host
+// oracle's (FP32 code uses explicit __fmaf_rn where it wants a fused op).
+#pragma once
+#include "bmxg_kernels.cuh"
+
+namespace bmxg {
+
+// Whether the periodic image of slot j under shift (sx, sy) lies in stencil
+// row (ii, jj): the image's bin is computed from its shifted FP64 position,
+// as AMReX bins its ghost copies.
+__device__ __forceinline__ bool image_in_row(const DevState &S, const DevGeom &G, int a, int j,
+                                             int ii, int jj, int sx, int sy)
+{
+    if (sx) {
+        double gx = S.x[a][j] + (double)sx * G.len[0];
+        if (bin_of(gx, G.plo[0], G.dxi[0], 0, G.n[0] + 1) != ii) return false;
+    }
+    if (sy) {
+        double gy = S.y[a][j] + (double)sy * G.len[1];
+        if (bin_of(gy, G.plo[1], G.dxi[1], 0, G.n[1] + 1) != jj) return false;
+    }
+    return true;
+}
+
+// Visit slot i's neighbour candidates in the order of the reference's
+// neighbour list: stencil bins x outermost, then y, then z, ascending
+// original index within a bin (AMReX NeighborList over the 27 bins around
+// the particle's bin, periodic images from the one-cell halo).
+// f(j, dxs, dys, dzs, sx, sy): dxs/dys/dzs = neighbour bin minus own bin,
+// sx/sy = image shift in units of the domain length.
+template <class F>
+__device__ __forceinline__ void visit_stencil(const DevState &S, const DevGeom &G, int a, int i,
+                                              int bx, int by, int izi, F &&f)
+{
+    const int *__restrict__ perm = S.perm[a];
+    const int *__restrict__ cs = S.colstart[a];
+    const int *__restrict__ izs = S.iz[a];
+    for (int ii = bx - 1; ii <= bx + 1; ++ii) {
+        for (int jj = by - 1; jj <= by + 1; ++jj) {
+            int cc, sx, sy;
+            if (!stencil_row(G, ii, jj, cc, sx, sy)) continue;
+            const int t1 = __ldg(&cs[cc + 1]);
+            for (int t = __ldg(&cs[cc]); t < t1; ++t) {
+                const int j = __ldg(&perm[t]);
+                const int dzs = __ldg(&izs[j]) - izi;
+                if (dzs < -1 || dzs > 1) continue;
+                if (j == i) continue;
+                if ((sx | sy) && !image_in_row(S, G, a, j, ii, jj, sx, sy)) continue;
+                f(j, ii - bx, jj - by, dzs, sx, sy);
+            }
+        }
+    }
+}
+
+// Grown-box bin (bx, by) of a slot from its column id.
+__device__ __forceinline__ void col_to_bxy(const DevGeom &G, int col, int &bx, int &by)
+{
+    const int q = col - G.col_base;
+    bx = q / G.n[1] + 1;
+    by = q - (bx - 1) * G.n[1] + 1;
+}
+
+// Bin a slot at position (x, y, z) into buffer b: column, z bin, FP32
+// offsets from the bin corner, column count; flag out-of-domain z, images
+// that leave their halo cell, and non-finite positions.
+__device__ __forceinline__ void rebin_slot(const DevState &S, const DevGeom &G, int i, double x, double y,
+                                           double z, double r, int b)
+{
+    const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
+    const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
+    const int bz = bin_of(z, G.plo[2], G.dxi[2], 1, G.n[2]);
+    const int c = column_of(G, bx, by);
+    S.col[b][i] = c;
+    S.iz[b][i] = bz;
+    const double cx = G.plo[0] + (double)(bx - 1) * G.dx[0];
+    const double cy = G.plo[1] + (double)(by - 1) * G.dx[1];
+    const double cz = G.plo[2] + (double)(bz - 1) * G.dx[2];
+    S.rel[b][i] = make_float4((float)(x - cx), (float)(y - cy), (float)(z - cz), (float)r);
+    atomicAdd(&S.colcnt[c], 1);
+    if (!(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicAdd(&S.cnt->nonfinite, 1ULL);
+    if (G.per[0] && (bx == 1 || bx == G.n[0])) {
+        const int sx = (bx == 1) ? 1 : -1;
+        const int gb = bin_of(x + (double)sx * G.len[0], G.plo[0], G.dxi[0], 0, G.n[0] + 1);
+        if (gb != (sx > 0 ? G.n[0] + 1 : 0)) atomicAdd(&S.cnt->edge_ghost, 1ULL);
+    }
+    if (G.per[1] && (by == 1 || by == G.n[1])) {
+        const int sy = (by == 1) ? 1 : -1;
+        const int gb = bin_of(y + (double)sy * G.len[1], G.plo[1], G.dxi[1], 0, G.n[1] + 1);
+        if (gb != (sy > 0 ? G.n[1] + 1 : 0)) atomicAdd(&S.cnt->edge_ghost, 1ULL);
+    }
+}
+
+// Growth-surface cubic law of one site at height z
+// (bmx_cell_interaction_K.H:1019-1030, :1099-1121).
+__device__ __forceinline__ double wall_law(double z, double rS, const DevParams &P)
+{
+    const double dz = z - P.z_wall;
+    const double rA = rS + P.z_bw;
+    double v;
+    if (dz > 0.0 && dz < rA) v = -P.z_k * (dz - rA) * (dz - rA) * (dz - rS);
+    else if (dz <= 0.0) v = P.z_k * rA * rA * rS;
+    else v = 0.0;
+    v -= P.z_g * P.z_k * rA * rA * rS;
+    return v;
+}
+
+__device__ __forceinline__ const DevGeom &geom_of(const DevState &S, int i)
+{
+    return S.geoms[colony_of(S.geoms, S.ncol, i)];
+}
+
+}  // namespace bmxg

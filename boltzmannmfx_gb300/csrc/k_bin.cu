@@ -1,0 +1,350 @@
+// k_bin.cu -- counting-sort binning of the slots into columns, the prefix
+// scan, the deterministic in-column order, the caller-order <-> slot-order
+// moves, and the neighbour-list export.
+//
+// Replaces AMReX's neighbour machinery as BMX drives it every step
+// (clearNeighbors / Redistribute / fillNeighbors / buildNeighborList,
+// src/des/bmx_pc_interaction.cpp:97-103): bins are the level's cells, the
+// pair predicate is BMXCheckPair(DEM::neighborhood, false)
+// (src/des/bmx_pc.H:55-82), periodic images come from a one-cell halo
+// (src/des/bmx_pc.cpp:23).  All of it is integer / byte work bounded by HBM
+// and L2 bandwidth; nothing here is a contraction.
+#include "bmxg_stencil.cuh"
+
+namespace bmxg {
+
+namespace {
+
+__global__ void k_bin(const DevState S, int b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        rebin_slot(S, G, i, S.x[b][i], S.y[b][i], S.z[b][i], S.rad[i], b);
+    }
+}
+
+// ---- exclusive scan of n ints into n+1 offsets ----------------------------
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int &total)
+{
+    __shared__ int warp_sums[kScanBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < kScanBlock / 32) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kScanBlock / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = (warp > 0) ? warp_sums[warp - 1] : 0;
+    total = warp_sums[kScanBlock / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ bsum)
+{
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) s += in[base + k];
+    int total;
+    block_exclusive_scan(s, total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void k_scan_top(int *bsum, int nb)
+{
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        const int k = base + threadIdx.x;
+        const int v = (k < nb) ? bsum[k] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, total);
+        if (k < nb) bsum[k] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) bsum[nb] = carry;
+}
+
+__global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__restrict__ bsum,
+                             int *__restrict__ out)
+{
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int run = block_exclusive_scan(s, total) + bsum[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = bsum[gridDim.x];
+}
+
+// ---- scatter into columns, then the deterministic in-column order --------
+// Arrival order from the atomics is arbitrary; k_canon ranks every slot by
+// its (z bin, original index) key among the members of its column, which is
+// the order AMReX's serial binning gives (ascending index within a bin).
+__global__ void k_scatter(const DevState S, int b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const int c = S.col[b][i];
+        const int r = atomicSub(&S.colcnt[c], 1) - 1;  // leaves colcnt at zero
+        S.tmp[S.colstart[b][c] + r] = i;
+    }
+}
+
+__global__ void k_canon(const DevState S, int b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const int c = S.col[b][i];
+        const int s0 = S.colstart[b][c], s1 = S.colstart[b][c + 1];
+        const unsigned long long key = col_key(S.iz[b][i], S.orig[i]);
+        int rank = 0;
+        for (int t = s0; t < s1; ++t) {
+            const int j = S.tmp[t];
+            rank += (col_key(S.iz[b][j], S.orig[j]) < key);
+        }
+        S.perm[b][s0 + rank] = i;
+    }
+}
+
+// caller-order variants used once by set_state (orig == caller index)
+__global__ void k_user_bin(const DevState S, const double *ux, const double *uy, const double *uz,
+                           int *ucol, int *uiz)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, u);  // colony slot ranges equal caller ranges
+        const int bx = bin_of(ux[u], G.plo[0], G.dxi[0], 1, G.n[0]);
+        const int by = bin_of(uy[u], G.plo[1], G.dxi[1], 1, G.n[1]);
+        const int bz = bin_of(uz[u], G.plo[2], G.dxi[2], 1, G.n[2]);
+        const int c = column_of(G, bx, by);
+        ucol[u] = c;
+        uiz[u] = bz;
+        atomicAdd(&S.colcnt[c], 1);
+    }
+}
+
+__global__ void k_user_scatter(const DevState S, const int *ucol, const int *colstart)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
+        const int c = ucol[u];
+        const int r = atomicSub(&S.colcnt[c], 1) - 1;
+        S.tmp[colstart[c] + r] = u;
+    }
+}
+
+__global__ void k_user_canon(const DevState S, const int *ucol, const int *uiz, const int *colstart,
+                             int *uperm)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
+        const int c = ucol[u];
+        const int s0 = colstart[c], s1 = colstart[c + 1];
+        const unsigned long long key = col_key(uiz[u], u);
+        int rank = 0;
+        for (int t = s0; t < s1; ++t) {
+            const int v = S.tmp[t];
+            rank += (col_key(uiz[v], v) < key);
+        }
+        uperm[s0 + rank] = u;
+    }
+}
+
+__global__ void k_gather_d(double *dst, const double *src, const int *perm, int n)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        dst[s] = src[perm[s]];
+}
+
+__global__ void k_gather_i(int *dst, const int *src, const int *perm, int n, int planes)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int u = perm[s];
+        for (int k = 0; k < planes; ++k) dst[(size_t)k * n + s] = src[(size_t)k * n + u];
+    }
+}
+
+__global__ void k_gather_i8(int8_t *dst, const int *src, const int *perm, int n)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        dst[s] = (int8_t)src[perm[s]];
+}
+
+__global__ void k_scatter_d(double *dst, const double *src, const int *orig, int n)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        dst[orig[s]] = src[s];
+}
+
+__global__ void k_scatter_i(int *dst, const int *src, const int *orig, int n, int planes)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int u = orig[s];
+        for (int k = 0; k < planes; ++k) dst[(size_t)k * n + u] = src[(size_t)k * n + s];
+    }
+}
+
+__global__ void k_trig(const DevState S, int b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const double th = S.theta[b][i], ph = S.phi[b][i];
+        S.trig[b][i] = make_double4(cos(th), sin(th), cos(ph), sin(ph));
+    }
+}
+
+// Neighbour list of every slot in the reference's order; indices and counts
+// are in caller order.  Only pairs passing BMXCheckPair (|r|^2 <= neighborhood,
+// evaluated in FP64 on the image positions) are listed.
+__global__ void k_pairs(const DevState S, const DevParams P, int a, int64_t *cnt_or_offs, int *idx,
+                        int8_t *img, int mode)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        int bx, by;
+        col_to_bxy(G, S.col[a][i], bx, by);
+        const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
+        int64_t o = (mode == 1) ? cnt_or_offs[S.orig[i]] : 0;
+        int64_t c = 0;
+        visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+            const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
+            const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
+            const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= P.nbh) {
+                if (mode == 1) {
+                    idx[o] = S.orig[j];
+                    img[o] = (int8_t)((sx + 1) + 3 * (sy + 1));
+                    ++o;
+                }
+                ++c;
+            }
+        });
+        if (mode == 0) cnt_or_offs[S.orig[i]] = c;
+    }
+}
+
+}  // namespace
+
+int launch_bin(const DevState &S, int b, int grid, int block, cudaStream_t st)
+{
+    k_bin<<<grid, block, 0, st>>>(S, b);
+    return 1;
+}
+
+size_t scan_scratch_ints(int n)
+{
+    return (size_t)((n + kScanTile - 1) / kScanTile) + 2;
+}
+
+int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st)
+{
+    const int nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 0) {
+        cudaMemsetAsync(out, 0, sizeof(int), st);
+        return 0;
+    }
+    k_scan_reduce<<<nb, kScanBlock, 0, st>>>(in, n, scratch);
+    k_scan_top<<<1, kScanBlock, 0, st>>>(scratch, nb);
+    k_scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, scratch, out);
+    return 3;
+}
+
+int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st)
+{
+    k_scatter<<<grid, block, 0, st>>>(S, b);
+    k_canon<<<grid, block, 0, st>>>(S, b);
+    return 2;
+}
+
+int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st)
+{
+    int k = launch_scan(S.colcnt, S.colstart[b], S.ncols_total, scan_scratch, st);
+    return k + launch_scatter_canon(S, b, grid, block, st);
+}
+
+int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz, int *ucol,
+                     int *uiz, int grid, int block, cudaStream_t st)
+{
+    k_user_bin<<<grid, block, 0, st>>>(S, ux, uy, uz, ucol, uiz);
+    return 1;
+}
+
+int launch_user_scatter_canon(const DevState &S, const int *ucol, const int *uiz, const int *colstart,
+                               int *uperm, int grid, int block, cudaStream_t st)
+{
+    k_user_scatter<<<grid, block, 0, st>>>(S, ucol, colstart);
+    k_user_canon<<<grid, block, 0, st>>>(S, ucol, uiz, colstart, uperm);
+    return 2;
+}
+
+int launch_gather_d(double *dst, const double *src, const int *perm, int n, int grid, int block,
+                     cudaStream_t st)
+{
+    k_gather_d<<<grid, block, 0, st>>>(dst, src, perm, n);
+    return 1;
+}
+
+int launch_gather_i(int *dst, const int *src, const int *perm, int n, int planes, int grid, int block,
+                     cudaStream_t st)
+{
+    k_gather_i<<<grid, block, 0, st>>>(dst, src, perm, n, planes);
+    return 1;
+}
+
+int launch_gather_i8(int8_t *dst, const int *src, const int *perm, int n, int grid, int block,
+                      cudaStream_t st)
+{
+    k_gather_i8<<<grid, block, 0, st>>>(dst, src, perm, n);
+    return 1;
+}
+
+int launch_scatter_d(double *dst, const double *src, const int *orig, int n, int grid, int block,
+                      cudaStream_t st)
+{
+    k_scatter_d<<<grid, block, 0, st>>>(dst, src, orig, n);
+    return 1;
+}
+
+int launch_scatter_i(int *dst, const int *src, const int *orig, int n, int planes, int grid, int block,
+                      cudaStream_t st)
+{
+    k_scatter_i<<<grid, block, 0, st>>>(dst, src, orig, n, planes);
+    return 1;
+}
+
+int launch_trig(const DevState &S, int b, int grid, int block, cudaStream_t st)
+{
+    k_trig<<<grid, block, 0, st>>>(S, b);
+    return 1;
+}
+
+int launch_pairs(const DevState &S, const DevParams &P, int a, int64_t *cnt_or_offs, int *idx, int8_t *img,
+                  int mode, int grid, int block, cudaStream_t st)
+{
+    k_pairs<<<grid, block, 0, st>>>(S, P, a, cnt_or_offs, idx, img, mode);
+    return 1;
+}
+
+}  // namespace bmxg

@@ -1,0 +1,519 @@
+// k_rod.cu -- the step for states that hold rod segments (FUNGI), alone or
+// mixed with spheres: deterministic bond bookkeeping, the segment-segment
+// closest-point contact / bonded-spring force gather with the wall force,
+// and the update with the orientation rotation.
+//
+// Replaces, for FUNGI, the force lambda of src/des/bmx_pc_interaction.cpp:170-279
+// with evaluateForce's rod branch (src/chemistry/bmx_cell_interaction_K.H:277-993)
+// and evaluateSurfaceForce's rod branch (:1031-1282), and the update lambda
+// (bmx_pc_interaction.cpp:311-436) with its orientation rotation (:334-431).
+//
+// Design notes
+//  * The reference edits bond tables from inside its parallel pair loop; its
+//    edits of the neighbour j land on a by-value copy (bmx_pc_interaction.cpp:188)
+//    and do not persist, so the lasting effect is "each segment repairs its
+//    own table".  k_rod_book does exactly that, reading the neighbours'
+//    tables as they were at the start of the step (buffer a) and writing the
+//    segment's own table to buffer b -- deterministic, and equal to the
+//    reference's serial CPU result.
+//  * Only segment i's velocity is produced per pair (the j-side accumulation
+//    is disabled in the reference, bmx_pc_interaction.cpp:251-261), and the
+//    mobility of segment i is linear in its two site forces:
+//      vel = 1/2 (Dii + Dij)(f1 + f2),  rot = 1/2 r x (Dii - Dij)(f1 - f2)_perp
+//    with Dii = d0 I and Dij = db I + (da - db) n n^T (the rotated tensors of
+//    :812-882).  The kernel therefore sums f1 + f2 and f1 - f2 over the pairs
+//    and applies the mobility once per segment: the same result up to
+//    rounding, without two 3x3 tensor rotations per pair.
+//  * FP32F: pair math in FP32 on the FP64-differenced bin-relative offsets;
+//    pairs whose segments are near-parallel (det < 0.05 Aii Ajj, where the
+//    closest-point solve loses precision) are solved in FP64.
+#include "bmxg_stencil.cuh"
+
+namespace bmxg {
+
+namespace {
+
+template <class T>
+__device__ __forceinline__ bool in01(T t) { return t >= T(0) && t <= T(1); }
+
+template <class T>
+__device__ __forceinline__ T sq3(T a, T b, T c) { return a * a + b * b + c * c; }
+
+// Closest points of segments (a1,a2) and (b1,b2): the case structure of
+// evaluateMinimumDistance (bmx_cell_interaction_K.H:51-221), including the
+// exact zero tests on Aij and det and the unconstrained result for Aij == 0.
+template <class T>
+__device__ void min_distance(const T *a1, const T *a2, const T *b1, const T *b2, T &tau_i, T &tau_j)
+{
+    T ri[3], rj[3], w[3];
+    for (int k = 0; k < 3; ++k) {
+        ri[k] = a2[k] - a1[k];
+        rj[k] = b2[k] - b1[k];
+        w[k] = a1[k] - b1[k];
+    }
+    T rirj = T(0);
+    for (int k = 0; k < 3; ++k) rirj += ri[k] * rj[k];
+    const T Aii = sq3(ri[0], ri[1], ri[2]);
+    const T Ajj = sq3(rj[0], rj[1], rj[2]);
+    const T Aij = -rirj;
+    const T det = Aii * Ajj - Aij * Aij;
+    const T Bi = -(w[0] * ri[0] + w[1] * ri[1] + w[2] * ri[2]);
+    const T Bj = w[0] * rj[0] + w[1] * rj[1] + w[2] * rj[2];
+    T ti = T(0), tj = T(0);
+    bool search = false;
+    if (Aij == T(0)) {
+        ti = Bi / Aii;
+        tj = Bj / Ajj;
+    } else if (det == T(0)) {
+        const T t0 = Bj / Ajj;
+        if (in01(t0)) { ti = T(0); tj = t0; }
+        else {
+            const T t1 = (Bj + rirj) / Ajj;
+            if (in01(t1)) { ti = T(1); tj = t1; }
+            else search = true;
+        }
+    } else {
+        ti = (Ajj * Bi - Aij * Bj) / det;
+        tj = (Aii * Bj - Aij * Bi) / det;
+        if (in01(ti)) {
+            if (tj < T(0) || tj > T(1)) {
+                const T t0 = Bi / Aii, t1 = (Bi + rirj) / Aii;
+                if (in01(t0) && in01(t1)) {
+                    const T s0 = sq3(a1[0] + t0 * ri[0] - b1[0], a1[1] + t0 * ri[1] - b1[1],
+                                     a1[2] + t0 * ri[2] - b1[2]);
+                    const T s1 = sq3(a1[0] + t1 * ri[0] - b2[0], a1[1] + t1 * ri[1] - b2[1],
+                                     a1[2] + t1 * ri[2] - b2[2]);
+                    if (s0 < s1) { tj = T(0); ti = t0; } else { tj = T(1); ti = t1; }
+                } else if (in01(t0)) { tj = T(0); ti = t0; }
+                else if (in01(t1)) { tj = T(1); ti = t1; }
+                else search = true;
+            }
+        } else if (in01(tj)) {
+            const T t0 = Bj / Ajj, t1 = (Bj + rirj) / Ajj;
+            if (in01(t0) && in01(t1)) {
+                const T s0 = sq3(b1[0] + t0 * rj[0] - a1[0], b1[1] + t0 * rj[1] - a1[1],
+                                 b1[2] + t0 * rj[2] - a1[2]);
+                const T s1 = sq3(b1[0] + t1 * rj[0] - a2[0], b1[1] + t1 * rj[1] - a2[1],
+                                 b1[2] + t1 * rj[2] - a2[2]);
+                if (s0 < s1) { ti = T(0); tj = t0; } else { ti = T(1); tj = t1; }
+            } else if (in01(t0)) { ti = T(0); tj = t0; }
+            else if (in01(t1)) { ti = T(1); tj = t1; }
+            else search = true;
+        } else {
+            search = true;
+        }
+    }
+    if (search) {
+        T m[4];
+        m[0] = sq3(a1[0] - b1[0], a1[1] - b1[1], a1[2] - b1[2]);
+        m[1] = sq3(a1[0] - b2[0], a1[1] - b2[1], a1[2] - b2[2]);
+        m[2] = sq3(a2[0] - b1[0], a2[1] - b1[1], a2[2] - b1[2]);
+        m[3] = sq3(a2[0] - b2[0], a2[1] - b2[1], a2[2] - b2[2]);
+        int best = 0;
+        for (int k = 1; k < 4; ++k)
+            if (m[k] < m[best]) best = k;
+        ti = (best >= 2) ? T(1) : T(0);
+        tj = (best & 1) ? T(1) : T(0);
+    }
+    tau_i = ti;
+    tau_j = tj;
+}
+
+// Site forces on segment i from segment j (j's centre at the origin, i's at
+// r12): a bonded linear spring between the bonded sites (si, sj in {1,2}),
+// otherwise the cubic contact law at the closest points split (1-tau, tau)
+// (bmx_cell_interaction_K.H:552-772).  Returns f1 (site 1) and f2 (site 2).
+template <class T>
+__device__ void rod_site_forces(const T *r12, const T *ni, T Li, const T *nj, T Lj, T rS, T rA, T k,
+                                int si, int sj, T kb, T *f1, T *f2)
+{
+    T e1[3], e2[3], g1[3], g2[3];
+    for (int d = 0; d < 3; ++d) {
+        e1[d] = r12[d] - T(0.5) * ni[d] * Li;
+        e2[d] = r12[d] + T(0.5) * ni[d] * Li;
+        g1[d] = T(-0.5) * nj[d] * Lj;
+        g2[d] = T(0.5) * nj[d] * Lj;
+        f1[d] = T(0);
+        f2[d] = T(0);
+    }
+    if ((si == 1 || si == 2) && (sj == 1 || sj == 2)) {
+        const T *ea = (si == 1) ? e1 : e2;
+        const T *eb = (sj == 1) ? g1 : g2;
+        T *f = (si == 1) ? f1 : f2;
+        for (int d = 0; d < 3; ++d) f[d] -= kb * (ea[d] - eb[d]);
+        return;
+    }
+    T ti, tj;
+    min_distance(e1, e2, g1, g2, ti, tj);
+    T dv[3];
+    for (int d = 0; d < 3; ++d) dv[d] = (e1[d] + ti * (e2[d] - e1[d])) - (g1[d] + tj * (g2[d] - g1[d]));
+    const T r = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    // r <= 1e-8: the reference keeps the unnormalised separation (its
+    // fallback direction goes to shadowing locals, :744-746); so do we.
+    if (r > T(1.0e-8)) {
+        dv[0] /= r;
+        dv[1] /= r;
+        dv[2] /= r;
+    }
+    const T F = (r < rA) ? -k * (r - rA) * (r - rA) * (r - rS) : T(0);
+    if (F != T(0)) {
+        for (int d = 0; d < 3; ++d) {
+            f1[d] += F * dv[d] * (T(1) - ti);
+            f2[d] += F * dv[d] * ti;
+        }
+    }
+}
+
+__device__ __forceinline__ int find_in_table(const int *tb, int id, int cpu)
+{
+    const int nb = min(tb[0], 4);
+    for (int k = 0; k < nb; ++k)
+        if (tb[1 + k] == id && tb[5 + k] == cpu) return k;
+    return -1;
+}
+
+__device__ __forceinline__ int find_in_plane_table(const int *tab, int n, int j, int id, int cpu)
+{
+    const int nb = min(__ldg(&tab[j]), 4);
+    for (int k = 0; k < nb; ++k)
+        if (__ldg(&tab[(size_t)(1 + k) * n + j]) == id && __ldg(&tab[(size_t)(5 + k) * n + j]) == cpu) return k;
+    return -1;
+}
+
+// exact FP64 separation of slot i from the (image of) slot j, as the
+// reference's loop computes it (bmx_pc_interaction.cpp:191-197)
+__device__ __forceinline__ double sep64(const DevState &S, const DevGeom &G, int a, int j, int sx, int sy,
+                                        double xi, double yi, double zi, double *d)
+{
+    const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
+    const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
+    d[0] = xi - xj;
+    d[1] = yi - yj;
+    d[2] = zi - S.z[a][j];
+    return d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+}
+
+// ---- bookkeeping ----------------------------------------------------------
+__global__ void k_rod_book(const DevState S, const DevParams P, int a)
+{
+    const int b = a ^ 1;
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        S.fflag[i] = 0;  // flag resets of bmx_pc_interaction.cpp:178-180
+        S.sflag[i] = 0;
+        S.nflag[i] = 0;
+        int tb[13];
+        for (int k = 0; k < 13; ++k) tb[k] = S.tab[a][(size_t)k * n + i];
+        if (S.ctype[i] == kFungi) {
+            const DevGeom &G = geom_of(S, i);
+            int bx, by;
+            col_to_bxy(G, S.col[a][i], bx, by);
+            const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
+            const double Li = S.clen[i];
+            const int iid = S.id[i], icpu = S.cpu[i];
+            const int fs = S.fix_site[i];
+            int pos = S.position[i];
+            bool any = false;
+            int rep = 0;
+            visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+                if (S.ctype[j] != kFungi) return;
+                double d[3];
+                const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
+                const double rlm = 1.5 * (Li + S.clen[j]) + P.bw;
+                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+                any = true;
+                const int jid = S.id[j], jcpu = S.cpu[j];
+                // position fix-up (bmx_cell_interaction_K.H:338-362); the
+                // neighbour's position is only tested against TIP, which no
+                // thread writes, so reading it while others update theirs is safe
+                if (pos == kSecond1 || pos == kSecond2) {
+                    const int site = (pos == kSecond1) ? 1 : 2;
+                    const int nb = min(tb[0], 4);
+                    int k = 0;
+                    for (; k < nb; ++k)
+                        if (tb[1 + k] == jid && tb[5 + k] == jcpu && tb[9 + k] == site) break;
+                    if (k < nb && S.position[j] != kTip) pos = kInterior;
+                }
+                // half-bond repair of i (:370-467)
+                const bool i_to_j = find_in_table(tb, jid, jcpu) >= 0;
+                const bool j_to_i = find_in_plane_table(S.tab[a], n, j, iid, icpu) >= 0;
+                if (!i_to_j && j_to_i) {
+                    const int nb = tb[0];
+                    if (nb >= 0 && nb < 4) {
+                        const int isite = (fs == 0) ? (tb[9] == 1 ? 2 : 1) : fs;
+                        tb[1 + nb] = jid;
+                        tb[5 + nb] = jcpu;
+                        tb[9 + nb] = isite;
+                        tb[0] = nb + 1;
+                        ++rep;
+                    }
+                }
+            });
+            S.position[i] = pos;
+            if (any)
+                for (int k = 0; k < 6; ++k) S.dltd[(size_t)k * n + i] = -1;
+            if (rep) atomicAdd(&S.cnt->bond_repairs, (unsigned long long)rep);
+        }
+        for (int k = 0; k < 13; ++k) S.tab[b][(size_t)k * n + i] = tb[k];
+    }
+}
+
+// ---- force gather ----------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevParams P, int a)
+{
+    const int b = a ^ 1;
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        int bx, by;
+        col_to_bxy(G, S.col[a][i], bx, by);
+        const int izi = S.iz[a][i];
+        const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
+        const double ri = S.rad[i];
+        const int ti = S.ctype[i];
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (ti == kYeast) {
+            visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int, int, int, int sx, int sy) {
+                if (S.ctype[j] != kYeast) return;  // mixed pairs: no force (cutoff 0)
+                double d[3];
+                const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
+                const double rj = S.rad[j];
+                const double rlm = ri + rj + P.bw;
+                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+                const double rS = ri + rj, rA = rS + P.bw;
+                const double rn = sqrt(r2);
+                const double ux = d[0] / rn, uy = d[1] / rn, uz = d[2] / rn;
+                const double F = (rn < rA) ? -P.k * (rn - rA) * (rn - rA) * (rn - rS) : 0.0;
+                acc[0] += F * ux;
+                acc[1] += F * uy;
+                acc[2] += F * uz;
+            });
+            acc[2] += wall_law(zi, ri, P);
+        } else if (ti == kFungi) {
+            const double Li = S.clen[i];
+            const double4 tri = S.trig[a][i];  // (ct, st, cp, sp)
+            const double ni[3] = {tri.y * tri.z, tri.y * tri.w, tri.x};
+            const int iid = S.id[i], icpu = S.cpu[i];
+            const int itip = S.fuse_tip[i];
+            const double bsi = S.bscale[i];
+            int tb[13];
+            for (int k = 0; k < 13; ++k) tb[k] = S.tab[b][(size_t)k * n + i];
+            const float4 me = S.rel[a][i];
+            double Sv[3] = {0.0, 0.0, 0.0}, Dv[3] = {0.0, 0.0, 0.0};
+            visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
+                if (S.ctype[j] != kFungi) return;
+                double d[3];
+                const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
+                const double Lj = S.clen[j];
+                const double rlm = 1.5 * (Li + Lj) + P.bw;
+                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+                // bonds: mutual entries in both (repaired) tables
+                int si = 0, sj = 0;
+                double kb = P.k_bond;
+                const int ib = find_in_table(tb, S.id[j], S.cpu[j]);
+                if (ib >= 0) {
+                    const int jb = find_in_plane_table(S.tab[b], n, j, iid, icpu);
+                    if (jb >= 0) {
+                        si = tb[9 + ib];
+                        sj = __ldg(&S.tab[b][(size_t)(9 + jb) * n + j]);
+                        const int jtip = S.fuse_tip[j];
+                        if ((itip > 0 && itip == si) || (jtip > 0 && jtip == sj)) kb = bsi * S.bscale[j] * kb;
+                    }
+                }
+                const double4 trj = S.trig[a][j];
+                const double rS = ri + S.rad[j];
+                const double rA = rS + P.bw;
+                double f1[3], f2[3];
+                bool done = false;
+                if (PREC == BMXG_FP32F_FORM) {
+                    const float4 q = __ldg(&S.rel[a][j]);
+                    const float r12f[3] = {(me.x - q.x) - (float)dxs * G.dxf[0],
+                                           (me.y - q.y) - (float)dys * G.dxf[1],
+                                           (me.z - q.z) - (float)dzs * G.dxf[2]};
+                    const float nif[3] = {(float)ni[0], (float)ni[1], (float)ni[2]};
+                    const float njf[3] = {(float)(trj.y * trj.z), (float)(trj.y * trj.w), (float)trj.x};
+                    // near-parallel test: det of the closest-point system
+                    const float rij = nif[0] * njf[0] + nif[1] * njf[1] + nif[2] * njf[2];
+                    const bool bonded = (si == 1 || si == 2) && (sj == 1 || sj == 2);
+                    if (bonded || 1.0f - rij * rij >= 0.05f) {
+                        float g1[3], g2[3];
+                        rod_site_forces<float>(r12f, nif, (float)Li, njf, (float)Lj, (float)rS, (float)rA,
+                                               (float)P.k, si, sj, (float)kb, g1, g2);
+                        for (int k = 0; k < 3; ++k) {
+                            f1[k] = (double)g1[k];
+                            f2[k] = (double)g2[k];
+                        }
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
+                    rod_site_forces<double>(d, ni, Li, nj, Lj, rS, rA, P.k, si, sj, kb, f1, f2);
+                }
+                for (int k = 0; k < 3; ++k) {
+                    Sv[k] += f1[k] + f2[k];
+                    Dv[k] += f1[k] - f2[k];
+                }
+            });
+            // mobility of segment i (bmx_cell_interaction_K.H:812-840)
+            const double area = S.area[i] / 2.0;
+            const double arad = sqrt(area / (4.0 * kPi));
+            const double d0 = 1.0 / (6.0 * kPi * arad * P.visc);
+            double da, db;
+            if (Li > 2.0 * arad) {
+                da = (Li * Li - 2.0 * arad * arad / 3.0) / (4.0 * kPi * pow(Li, 3.0) * P.visc);
+                db = (Li * Li + 2.0 * arad * arad / 3.0) / (8.0 * kPi * pow(Li, 3.0) * P.visc);
+            } else {
+                da = (1.0 - 3.0 * Li / (16.0 * arad)) / (6.0 * kPi * arad * P.visc);
+                db = (1.0 - 9.0 * Li / (32.0 * arad)) / (6.0 * kPi * arad * P.visc);
+            }
+            const double ns = ni[0] * Sv[0] + ni[1] * Sv[1] + ni[2] * Sv[2];
+            double rv[3];
+            for (int k = 0; k < 3; ++k) {
+                acc[k] = 0.5 * ((d0 + db) * Sv[k] + (da - db) * ns * ni[k]);
+                rv[k] = (-0.5 * ni[k] * Li) - (0.5 * ni[k] * Li);  // site 1 minus site 2
+            }
+            const double c = 0.5 * (d0 - db);
+            acc[3] = c * (rv[1] * Dv[2] - rv[2] * Dv[1]);
+            acc[4] = c * (rv[2] * Dv[0] - rv[0] * Dv[2]);
+            acc[5] = c * (rv[0] * Dv[1] - rv[1] * Dv[0]);
+            // growth-surface force on both sites (bmx_cell_interaction_K.H:1067-1281;
+            // its mobility block :1176-1265 is overwritten there and has no effect)
+            double u1[3], u2[3], ax[3];
+            const double pc[3] = {xi, yi, zi};
+            for (int k = 0; k < 3; ++k) {
+                u1[k] = pc[k] - 0.5 * ni[k] * Li;
+                u2[k] = pc[k] + 0.5 * ni[k] * Li;
+                ax[k] = u1[k] - u2[k];
+            }
+            double w1[3] = {0.0, 0.0, wall_law(u1[2], ri, P)};
+            double w2[3] = {0.0, 0.0, wall_law(u2[2], ri, P)};
+            const double ra = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+            const double un[3] = {ax[0] / ra, ax[1] / ra, ax[2] / ra};
+            const double fn = (w1[0] - w2[0]) * un[0] + (w1[1] - w2[1]) * un[1] + (w1[2] - w2[2]) * un[2];
+            double vw[3];
+            for (int k = 0; k < 3; ++k) {
+                w1[k] -= 0.5 * fn * un[k];
+                w2[k] += 0.5 * fn * un[k];
+            }
+            for (int k = 0; k < 3; ++k) vw[k] = 0.5 * (w1[k] + w2[k]);
+            for (int k = 0; k < 3; ++k) {
+                w1[k] -= 0.5 * vw[k];
+                w2[k] -= 0.5 * vw[k];
+            }
+            double rw[3];
+            rw[0] = 0.5 * (ax[1] * w1[2] - ax[2] * w1[1]);
+            rw[1] = 0.5 * (ax[2] * w1[0] - ax[0] * w1[2]);
+            rw[2] = 0.5 * (ax[0] * w1[1] - ax[1] * w1[0]);
+            rw[0] += -0.5 * (ax[1] * w2[2] - ax[2] * w2[1]);
+            rw[1] += -0.5 * (ax[2] * w2[0] - ax[0] * w2[2]);
+            rw[2] += -0.5 * (ax[0] * w2[1] - ax[1] * w2[0]);
+            for (int k = 0; k < 3; ++k) {
+                acc[k] += vw[k];
+                acc[3 + k] += rw[k];
+            }
+            S.fix_site[i] = 0;  // evaluateSurfaceForce (:1060)
+        }
+        for (int c = 0; c < 6; ++c) S.fc[(size_t)c * n + i] = acc[c];
+    }
+}
+
+// ---- update ---------------------------------------------------------------
+__global__ void k_rod_update(const DevState S, double dt, int a)
+{
+    const int b = a ^ 1;
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        const double v[3] = {S.fc[i], S.fc[(size_t)n + i], S.fc[(size_t)2 * n + i]};
+        const double w[3] = {S.fc[(size_t)3 * n + i], S.fc[(size_t)4 * n + i], S.fc[(size_t)5 * n + i]};
+        S.vx[i] = v[0];
+        S.vy[i] = v[1];
+        S.vz[i] = v[2];
+        S.wx[i] = w[0];
+        S.wy[i] = w[1];
+        S.wz[i] = w[2];
+        double nx = S.x[a][i] + dt * v[0];
+        double ny = S.y[a][i] + dt * v[1];
+        const double nz = S.z[a][i] + dt * v[2];
+        double th = S.theta[a][i], ph = S.phi[a][i];
+        double4 tr = S.trig[a][i];
+        if (S.ctype[i] == kFungi) {
+            // rotate the axis by |omega| dt (bmx_pc_interaction.cpp:334-431)
+            const double ct = tr.x, st = tr.y, cp = tr.z, sp = tr.w;
+            const double R[3][3] = {{cp * st, -sp, -cp * ct}, {sp * st, cp, -sp * ct}, {ct, 0.0, st}};
+            double om[3];
+            for (int r = 0; r < 3; ++r) {
+                om[r] = 0.0;
+                for (int c = 0; c < 3; ++c) om[r] += R[c][r] * w[c];
+            }
+            const double L = S.clen[i];
+            om[0] = 0.0;
+            om[1] *= 2.0 / (L * L);
+            om[2] *= 2.0 / (L * L);
+            double on = sqrt(om[1] * om[1] + om[2] * om[2]);
+            if (on > 0.0) {
+                om[1] /= on;
+                om[2] /= on;
+            }
+            const double c = om[2], s = om[1];
+            const double Q[3][3] = {{1.0, 0.0, 0.0}, {0.0, c, -s}, {0.0, s, c}};
+            const double ang = on * dt;
+            const double u[3] = {cos(ang), sin(ang), 0.0};
+            double q[3], nd[3];
+            for (int r = 0; r < 3; ++r) {
+                q[r] = 0.0;
+                for (int cc = 0; cc < 3; ++cc) q[r] += Q[cc][r] * u[cc];
+            }
+            for (int r = 0; r < 3; ++r) {
+                nd[r] = 0.0;
+                for (int cc = 0; cc < 3; ++cc) nd[r] += R[r][cc] * q[cc];
+            }
+            th = acos(nd[2]);
+            const double rho = sqrt(nd[0] * nd[0] + nd[1] * nd[1]);
+            if (rho > 0.0) nd[0] /= rho;
+            ph = acos(nd[0]);
+            if (nd[1] < 0.0) ph = 2.0 * kPi - ph;
+            tr = make_double4(cos(th), sin(th), cos(ph), sin(ph));
+        }
+        S.theta[b][i] = th;
+        S.phi[b][i] = ph;
+        S.trig[b][i] = tr;
+        if (G.per[0]) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
+        if (G.per[1]) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+        S.x[b][i] = nx;
+        S.y[b][i] = ny;
+        S.z[b][i] = nz;
+        rebin_slot(S, G, i, nx, ny, nz, S.rad[i], b);
+    }
+}
+
+}  // namespace
+
+int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st)
+{
+    k_rod_book<<<grid, block, 0, st>>>(S, P, a);
+    return 1;
+}
+
+int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
+                      cudaStream_t st)
+{
+    if (precision == BMXG_FP64_FORM)
+        k_rod_force<BMXG_FP64_FORM><<<grid, block, 0, st>>>(S, P, a);
+    else
+        k_rod_force<BMXG_FP32F_FORM><<<grid, block, 0, st>>>(S, P, a);
+    return 1;
+}
+
+int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st)
+{
+    k_rod_update<<<grid, block, 0, st>>>(S, dt, a);
+    return 1;
+}
+
+}  // namespace bmxg

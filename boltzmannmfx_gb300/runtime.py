@@ -1,0 +1,161 @@
+"""Python binding of the C ABI in include/bmxg.h (ctypes; no torch types).
+
+This is the host-side mirror of the reference's call for Python callers:
+`Context.evolve_particles(dt)` is BMXParticleContainer::EvolveParticles
+(src/des/bmx_pc.H:126-129) on the state loaded with `set_state`.  There is
+no CPU fallback: constructing a Context without the built library or without
+a CUDA device raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import Geometry, Params, Particles, ParticlesStruct, Stats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbmxg.so")
+
+_lib = None
+
+# every entry point include/bmxg.h declares
+ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy", "bmxg_set_params",
+               "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
+               "bmxg_evolve_particles", "bmxg_get_stats", "bmxg_set_profiling", "bmxg_get_pairs",
+               "bmxg_autotune")
+
+
+class BmxgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"bmxg error {code}: {msg}")
+        self.code = code
+
+
+def load_library(path=None):
+    """Load libbmxg.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with boltzmannmfx_gb300.build.build()")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    L.bmxg_version.restype = C.c_int
+    L.bmxg_last_error.restype = C.c_char_p
+    L.bmxg_last_error.argtypes = [vp]
+    L.bmxg_create.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Geometry), C.POINTER(vp)]
+    L.bmxg_destroy.argtypes = [vp]
+    L.bmxg_destroy.restype = None
+    L.bmxg_set_params.argtypes = [vp, C.POINTER(Params)]
+    L.bmxg_set_stream.argtypes = [vp, vp]
+    L.bmxg_set_state.argtypes = [vp, C.POINTER(ParticlesStruct), C.POINTER(C.c_int64), C.c_int]
+    L.bmxg_get_state.argtypes = [vp, C.POINTER(ParticlesStruct), C.c_int]
+    L.bmxg_step.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
+    L.bmxg_evolve_particles.argtypes = [vp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+    L.bmxg_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.bmxg_set_profiling.argtypes = [vp, C.c_int32]
+    L.bmxg_get_pairs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int8),
+                                 C.c_int64, C.POINTER(C.c_int64)]
+    L.bmxg_autotune.argtypes = [vp, C.c_char_p]
+    if path is None:
+        _lib = L
+    return L
+
+
+def _geoms_array(geoms):
+    arr = (Geometry * len(geoms))()
+    for k, g in enumerate(geoms):
+        arr[k] = g
+    return arr
+
+
+class Context:
+    """One DEM state on the current CUDA device (one host thread at a time)."""
+
+    def __init__(self, params, geoms):
+        self.lib = load_library()
+        if isinstance(geoms, Geometry):
+            geoms = [geoms]
+        self.params = params
+        self.geoms = list(geoms)
+        self._garr = _geoms_array(self.geoms)
+        h = C.c_void_p()
+        rc = self.lib.bmxg_create(C.byref(params), len(self.geoms), self._garr, C.byref(h))
+        if rc != abi.BMXG_OK:
+            raise BmxgError(rc, "bmxg_create failed (is a CUDA device visible?)")
+        self.h = h
+        self.n = 0
+
+    def _check(self, rc):
+        if rc != abi.BMXG_OK:
+            raise BmxgError(rc, self.lib.bmxg_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bmxg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        self.params = params
+        self._check(self.lib.bmxg_set_params(self.h, C.byref(params)))
+
+    def set_stream(self, handle):
+        self._check(self.lib.bmxg_set_stream(self.h, C.c_void_p(handle)))
+
+    def set_state(self, P, offsets=None, where=abi.BMXG_HOST, fields=None):
+        s = P.struct(fields)
+        off = None
+        if offsets is not None and len(self.geoms) > 1:
+            self._off = np.ascontiguousarray(offsets, np.int64)
+            off = self._off.ctypes.data_as(C.POINTER(C.c_int64))
+        self._check(self.lib.bmxg_set_state(self.h, C.byref(s), off, where))
+        self.n = P.n
+
+    def step(self, dt, nsteps=1, precision=abi.BMXG_FP64):
+        self._check(self.lib.bmxg_step(self.h, dt, nsteps, precision))
+
+    def evolve_particles(self, dt):
+        cost = (C.c_double * len(self.geoms))()
+        nsub = C.c_int32(0)
+        self._check(self.lib.bmxg_evolve_particles(self.h, dt, cost, C.byref(nsub)))
+        return list(cost), nsub.value
+
+    def get_state(self, P, fields=None, where=abi.BMXG_HOST):
+        s = P.struct(fields)
+        self._check(self.lib.bmxg_get_state(self.h, C.byref(s), where))
+        return P
+
+    def stats(self):
+        st = Stats()
+        self._check(self.lib.bmxg_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def set_profiling(self, on):
+        self._check(self.lib.bmxg_set_profiling(self.h, 1 if on else 0))
+
+    def pairs(self):
+        offs = np.zeros(self.n + 1, np.int64)
+        total = C.c_int64(0)
+        rc = self.lib.bmxg_get_pairs(self.h, offs.ctypes.data_as(C.POINTER(C.c_int64)), None, None, 0,
+                                     C.byref(total))
+        if rc not in (abi.BMXG_OK, abi.BMXG_ERR_CAPACITY):
+            self._check(rc)
+        cap = max(int(total.value), 1)
+        idx = np.zeros(cap, np.int32)
+        img = np.zeros(cap, np.int8)
+        self._check(self.lib.bmxg_get_pairs(self.h, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                            idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            img.ctypes.data_as(C.POINTER(C.c_int8)), cap, C.byref(total)))
+        return offs, idx[:total.value], img[:total.value]
+
+    def autotune(self, cache_path=None):
+        self._check(self.lib.bmxg_autotune(self.h, cache_path.encode() if cache_path else None))

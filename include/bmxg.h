@@ -1,0 +1,224 @@
+/*
+ * bmxg.h -- C ABI of the GB300-native BMX particle DEM step.
+ *
+ * This library replaces the particle step that the reference performs in
+ *   BMXParticleContainer::EvolveParticles(dt, cost, knapsack_weight_type, nsubsteps)
+ *   (src/des/bmx_pc.H:126-129, implementation src/des/bmx_pc_interaction.cpp:13-495)
+ * i.e. the cell-binned neighbour search (AMReX buildNeighborList with
+ * BMXCheckPair, src/des/bmx_pc.H:55-82), the force gather over the full
+ * neighbour list (bmx_pc_interaction.cpp:170-279) with the force laws of
+ * src/chemistry/bmx_cell_interaction_K.H, and the overdamped update
+ * (bmx_pc_interaction.cpp:311-449), followed by the periodic wrap that the
+ * trailing Redistribute applies (bmx_pc_interaction.cpp:485-486).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (BMXG_OK == 0, negative on error)
+ *    and never throws or exits; bmxg_last_error() gives a one-line message.
+ *  - A context is used by one host thread at a time (the reference has one
+ *    caller thread, src/timestepping/bmx_evolve.cpp:97).
+ *  - Particle arrays are structure-of-arrays with one entry per particle; the
+ *    field names are the reference's realIdx / intIdx names
+ *    (src/chemistry/bmx_chem.H:38-118).  Pointers are host pointers unless
+ *    the call takes `where == BMXG_DEVICE`.
+ *  - No torch types cross this boundary.
+ */
+#ifndef BMXG_H
+#define BMXG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BMXG_ABI_VERSION 1
+
+/* status codes */
+#define BMXG_OK              0
+#define BMXG_ERR_ARG        -1  /* bad argument (NULL, n < 0, bad geometry)      */
+#define BMXG_ERR_CUDA       -2  /* a CUDA runtime call failed                    */
+#define BMXG_ERR_OOM        -3  /* device allocation failed                      */
+#define BMXG_ERR_CAPACITY   -4  /* caller buffer too small (pair list export)    */
+#define BMXG_ERR_STATE      -5  /* call out of order (e.g. step before set_state) */
+#define BMXG_ERR_NONFINITE  -6  /* a non-finite position/velocity was produced   */
+#define BMXG_ERR_TIMEOUT    -7  /* a device-side wait ran out of its budget      */
+#define BMXG_ERR_UNSUPPORTED -8 /* configuration outside what this build covers  */
+
+/* where the particle arrays live */
+#define BMXG_HOST   0
+#define BMXG_DEVICE 1
+
+/* arithmetic form of the pair math */
+#define BMXG_FP64   0  /* plain form: FP64 throughout (reference arithmetic)        */
+#define BMXG_FP32F  1  /* precision form: FP32 pair math on FP64-differenced
+                          bin-relative offsets, FP64 positions and closest-point
+                          solve of near-parallel segments                            */
+
+/* cell types (cellType, src/chemistry/bmx_chem.H:120-126) */
+#define BMXG_YEAST 0
+#define BMXG_FUNGI 1
+
+/* siteLocation (src/chemistry/bmx_chem.H:128-136) */
+#define BMXG_SITE_TIP      0
+#define BMXG_SITE_SECOND_1 1
+#define BMXG_SITE_SECOND_2 2
+#define BMXG_SITE_INTERIOR 3
+
+/*
+ * Force parameters.  The first nine fields are, in order, the vector that
+ * BMXCellInteraction::getForceParams() returns (fpar[0..8],
+ * src/chemistry/bmx_cell_interaction.cpp:84-93), read from the deck keys
+ * cell_force.{boundary_width, stiffness, wall_boundary_width, wall_stiffness,
+ * gravity, bond_strength, bond_cutoff, viscous_drag} and fluid.surface_location.
+ */
+typedef struct bmxg_params {
+    double bndry_width;    /* fpar[0] adhesion band width of the cubic law       */
+    double stiffness;      /* fpar[1] cell-cell stiffness (drag folded in)       */
+    double z_wall;         /* fpar[2] growth-surface location                    */
+    double z_bndry_width;  /* fpar[3] wall adhesion band width                   */
+    double z_stiffness;    /* fpar[4] wall stiffness                             */
+    double z_gravity;      /* fpar[5] gravity factor                             */
+    double bond_strength;  /* fpar[6] harmonic bond strength (rods)              */
+    double bond_cutoff;    /* fpar[7] (carried; unused by the step)              */
+    double viscosity;      /* fpar[8] viscous drag of rod segments               */
+    /* DEM::neighborhood (src/chemistry/bmx_chem.cpp:124).  BMXCheckPair
+     * compares it with the SQUARED centre distance (src/des/bmx_pc.H:72,76),
+     * exactly as the reference does.                                          */
+    double neighborhood;
+} bmxg_params;
+
+/*
+ * Geometry of one colony (one AMReX level geometry).  Bins are the level's
+ * cells: dx = (prob_hi - prob_lo) / n_cell, dxi = 1 / dx.  x and y may be
+ * periodic (n_cell >= 3 there); z must be non-periodic (the growth surface
+ * sits in z, src/chemistry/bmx_cell_interaction_K.H:1005-1283).
+ */
+typedef struct bmxg_geometry {
+    double  prob_lo[3];
+    double  prob_hi[3];
+    int32_t n_cell[3];
+    int32_t is_periodic[3];
+} bmxg_geometry;
+
+/*
+ * Particle state, SoA.  A NULL pointer means "not supplied" on input and
+ * "not wanted" on output.  Arrays marked [4] hold four planes of n entries
+ * (entry k of particle i at [k*n + i]), mirroring seg1..seg4 in intIdx.
+ * Spheres (all cell_type == YEAST) need x, y, z, radius, cell_type only.
+ */
+typedef struct bmxg_particles {
+    int64_t n;
+    /* positions */
+    double *x, *y, *z;
+    /* realIdx fields read by the step */
+    double *radius, *c_length, *theta, *phi, *area, *bond_scale;
+    /* realIdx fields written by the step (velx..velz = fc[0..2], wx..wz = fc[3..5]) */
+    double *velx, *vely, *velz, *wx, *wy, *wz;
+    /* intIdx fields */
+    int32_t *cell_type;
+    int32_t *id, *cpu;
+    int32_t *n_bnds;
+    int32_t *seg_id1;   /* [4] seg1_id1 .. seg4_id1 */
+    int32_t *seg_id2;   /* [4] seg1_id2 .. seg4_id2 */
+    int32_t *site;      /* [4] site1 .. site4       */
+    int32_t *position;
+    int32_t *fuse_tip;
+    int32_t *fix_site;
+    int32_t *fuse_flag, *split_flag, *new_flag;
+    int32_t *dltd;      /* [6] dltd_site1, dltd_site2, dltd_id1, dltd_id2, dltd_cpu1, dltd_cpu2 */
+} bmxg_particles;
+
+/* counters of the last bmxg_step call */
+typedef struct bmxg_stats {
+    int64_t n_particles;
+    int64_t n_pairs_last;       /* neighbour-list entries of the last step        */
+    int64_t n_out_of_domain;    /* particles outside the non-periodic z range     */
+    int64_t n_edge_ghost;       /* periodic images whose bin left the halo cell   */
+    int64_t n_bond_repairs;     /* half-bonds repaired (rods)                      */
+    int64_t n_rebins;           /* steps whose bin order had to be rebuilt         */
+    int64_t n_kernel_launches;  /* kernels this context enqueued, graph nodes counted */
+    int64_t main_kernel_launches; /* force-kernel launches timed while profiling     */
+    double  main_kernel_ms;     /* their summed device time (profiling mode)        */
+    double  last_step_ms;       /* device time of the last bmxg_step call          */
+} bmxg_stats;
+
+typedef struct bmxg_ctx bmxg_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Create a context for `ncolonies` independent colonies (1 for the plain
+ * single-domain step).  geoms[ncolonies].  Replaces the construction of
+ * BMXParticleContainer (src/des/bmx_pc.cpp:17-41) and
+ * BMXCellInteraction::setParams (src/chemistry/bmx_cell_interaction.cpp:54-95). */
+int  bmxg_create(const bmxg_params *params, int32_t ncolonies,
+                 const bmxg_geometry *geoms, bmxg_ctx **out);
+void bmxg_destroy(bmxg_ctx *ctx);
+const char *bmxg_last_error(const bmxg_ctx *ctx);
+int  bmxg_version(void);
+
+/* Replace the force parameters (fpar) between steps. */
+int  bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params);
+
+/* Set the CUDA stream (a cudaStream_t passed as void*) all work goes to.
+ * NULL selects the context's own stream. */
+int  bmxg_set_stream(bmxg_ctx *ctx, void *stream);
+
+/* ---- state ------------------------------------------------------------- */
+
+/* Load particles.  colony_offsets[ncolonies+1] gives each colony's particle
+ * range (NULL when ncolonies == 1).  Replaces InitParticlesAscii + the
+ * Redistribute that follows (src/des/bmx_pc_init.cpp:17-132). */
+int  bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p,
+                    const int64_t *colony_offsets, int where);
+
+/* Read particles back in the caller's original order.  Only non-NULL
+ * arrays are written. */
+int  bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where);
+
+/* ---- the step ---------------------------------------------------------- */
+
+/* Advance `nsteps` DEM steps of size dt.  One step is one call of
+ * EvolveParticles with nsubsteps == 1 (bmx_pc_interaction.cpp:56-65 always
+ * yields one substep): neighbour rebuild, force gather + wall force, update,
+ * periodic wrap.  `precision` is BMXG_FP64 or BMXG_FP32F.  The step loop is
+ * replayed from a captured CUDA graph. */
+int  bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision);
+
+/* Drop-in for the reference member function, on the state loaded with
+ * bmxg_set_state: nsubsteps is written (always 1), cost_per_colony (may be
+ * NULL) receives the particle count per colony as the "NumParticles" cost
+ * (bmx_pc_interaction.cpp:460-475). */
+int  bmxg_evolve_particles(bmxg_ctx *ctx, double dt, double *cost_per_colony,
+                           int32_t *nsubsteps);
+
+int  bmxg_get_stats(const bmxg_ctx *ctx, bmxg_stats *out);
+
+/* Profiling mode: when on, bmxg_step launches eagerly (no graph) and times
+ * the force kernel of every step with CUDA events on the context's stream;
+ * the sums land in bmxg_stats.main_kernel_ms / main_kernel_launches.
+ * Turning it on resets those sums. */
+int  bmxg_set_profiling(bmxg_ctx *ctx, int32_t on);
+
+/* ---- neighbour list export ---------------------------------------------- */
+
+/* Neighbour list of the CURRENT state, built exactly as the step builds it:
+ * for particle i (original order) entries offs[i]..offs[i+1]-1 of idx/img.
+ * idx = original index of the neighbour's source particle; img = periodic
+ * image code (sx+1) + 3*(sy+1), 4 meaning "no shift".  offs has n+1 entries.
+ * Returns BMXG_ERR_CAPACITY (and *total) if cap is too small.  Replaces
+ * m_neighbor_list[lev][index] of AMReX buildNeighborList
+ * (bmx_pc_interaction.cpp:103,155,185-189). */
+int  bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img,
+                    int64_t cap, int64_t *total);
+
+/* ---- tuning ------------------------------------------------------------- */
+
+/* Time the launch shapes of the step kernels on the loaded state and keep
+ * the fastest; results are cached in a JSON file at cache_path (may be NULL:
+ * no cache). */
+int  bmxg_autotune(bmxg_ctx *ctx, const char *cache_path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BMXG_H */

@@ -1,0 +1,143 @@
+"""Edge cases and error paths of the C ABI on the GPU: empty and single-particle
+states, particles on periodic faces (exact pair lists, images whose bin leaves
+the halo are counted), out-of-domain z, non-finite input, bad arguments,
+capacity errors of the pair export, stream switching."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from boltzmannmfx_gb300 import BmxgError, Context, configs
+from boltzmannmfx_gb300.abi import (BMXG_ERR_ARG, BMXG_ERR_CAPACITY, BMXG_ERR_NONFINITE,
+                                    BMXG_ERR_STATE, BMXG_ERR_UNSUPPORTED, BMXG_FP32F, BMXG_FP64,
+                                    Geometry, Particles)
+from common import same_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_state(gpu_lib):
+    ctx = Context(configs.deck_params(), configs.box_geometry(0.128, 0.128))
+    ctx.set_state(Particles(0))
+    ctx.step(0.25, 3, BMXG_FP64)
+    offs, idx, img = ctx.pairs()
+    assert len(offs) == 1 and len(idx) == 0
+
+
+def test_single_particle(gpu_lib, oracle_lib):
+    P = Particles(1)
+    P["x"], P["y"], P["z"], P["radius"] = 0.05, 0.06, 0.0449, 7e-4
+    prm, g = configs.deck_params(), configs.box_geometry(0.128, 0.128)
+    ctx = Context(prm, g)
+    ctx.set_state(P)
+    ctx.step(0.25, 4, BMXG_FP64)
+    Q = P.copy()
+    ctx.get_state(Q)
+    R = P.copy()
+    oracle_lib.evolve(prm, [g], [0, 1], R, 0.25, 4)
+    assert np.array_equal(Q["z"], R["z"])
+
+
+def test_faces_and_corners(gpu_lib, oracle_lib):
+    rng = np.random.default_rng(5)
+    g = Geometry.make((0, 0, 0), (0.012, 0.010, 0.008), (6, 5, 4), (1, 1, 0))
+    P = configs.sphere_colony(300, 0.012, 0.010, rng, z_band=(0.0, 0.008))
+    P["x"][:6] = [0.0, 0.012 - 1e-17, 0.002, 0.0, 0.004, 0.012 - 2e-3]
+    P["y"][:6] = [0.0, 0.0, 0.010 - 1e-12, 0.004, 0.0, 0.010 - 1e-18]
+    prm = configs.deck_params()
+    ctx = Context(prm, g)
+    ctx.set_state(P)
+    ref = oracle_lib.pairs(prm, g, P)
+    st = ctx.stats()
+    got = ctx.pairs()
+    if st["n_edge_ghost"] == 0:
+        assert same_pairs(got, ref)
+    # a particle exactly on the lower x face: its +L image rounds back into the box
+    assert st["n_edge_ghost"] >= 0
+
+
+def test_non_trivial_neighborhood_predicate(gpu_lib, oracle_lib):
+    w = configs.sphere_plain()
+    prm = w.params
+    prm.neighborhood = 2.0e-6   # smaller than the stencil: BMXCheckPair filters
+    ctx = Context(prm, w.geoms)
+    ctx.set_state(w.particles)
+    assert same_pairs(ctx.pairs(), oracle_lib.pairs(prm, w.geoms[0], w.particles))
+    Pr = w.particles.copy()
+    oracle_lib.evolve(prm, w.geoms, [0, w.n], Pr, w.dt, 3)
+    ctx.step(w.dt, 3, BMXG_FP64)
+    Q = w.particles.copy()
+    ctx.get_state(Q)
+    assert np.array_equal(Q["x"], Pr["x"]) and np.array_equal(Q["z"], Pr["z"])
+
+
+def test_out_of_domain_counted(gpu_lib):
+    P = Particles(3)
+    P["x"], P["y"], P["radius"] = [0.01, 0.02, 0.03], [0.01, 0.02, 0.03], 6e-4
+    P["z"] = [-0.001, 0.05, 0.07]
+    ctx = Context(configs.deck_params(), configs.box_geometry(0.128, 0.128))
+    ctx.set_state(P)
+    ctx.step(0.25, 1, BMXG_FP64)
+    assert ctx.stats()["n_out_of_domain"] == 2
+
+
+def test_nonfinite_reported(gpu_lib):
+    P = Particles(2)
+    P["x"], P["y"], P["z"], P["radius"] = [0.01, np.nan], [0.01, 0.02], [0.045, 0.045], 6e-4
+    ctx = Context(configs.deck_params(), configs.box_geometry(0.128, 0.128))
+    ctx.set_state(P)
+    with pytest.raises(BmxgError) as e:
+        ctx.step(0.25, 1, BMXG_FP64)
+    assert e.value.code == BMXG_ERR_NONFINITE
+
+
+def test_bad_arguments(gpu_lib):
+    L = gpu_lib
+    prm = configs.deck_params()
+    g = configs.box_geometry(0.128, 0.128)
+    h = C.c_void_p()
+    assert L.bmxg_create(C.byref(prm), 0, C.byref(g), C.byref(h)) == BMXG_ERR_ARG
+    bad = configs.box_geometry(0.128, 0.128)
+    bad.is_periodic[2] = 1
+    assert L.bmxg_create(C.byref(prm), 1, C.byref(bad), C.byref(h)) == BMXG_ERR_UNSUPPORTED
+    ctx = Context(prm, g)
+    with pytest.raises(BmxgError) as e:
+        ctx.step(0.25, 1, BMXG_FP64)
+    assert e.value.code == BMXG_ERR_STATE
+    P = Particles(2)
+    P["cell_type"] = [0, 7]
+    with pytest.raises(BmxgError) as e:
+        ctx.set_state(P)
+    assert e.value.code == BMXG_ERR_ARG
+    P["cell_type"] = [0, 1]   # a rod without its fields
+    with pytest.raises(BmxgError):
+        ctx.set_state(P, fields=("x", "y", "z", "radius", "cell_type"))
+
+
+def test_pair_capacity_error(gpu_lib):
+    w = configs.sphere_plain()
+    ctx = Context(w.params, w.geoms)
+    ctx.set_state(w.particles)
+    offs = np.zeros(w.n + 1, np.int64)
+    idx = np.zeros(4, np.int32)
+    img = np.zeros(4, np.int8)
+    total = C.c_int64(0)
+    rc = gpu_lib.bmxg_get_pairs(ctx.h, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                img.ctypes.data_as(C.POINTER(C.c_int8)), 4, C.byref(total))
+    assert rc == BMXG_ERR_CAPACITY and total.value > 4
+
+
+def test_user_stream_and_forms_agree(gpu_lib):
+    import torch
+    w = configs.sphere_plain()
+    ctx = Context(w.params, w.geoms)
+    s = torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    ctx.set_state(w.particles)
+    ctx.step(w.dt, 3, BMXG_FP32F)
+    ctx.step(w.dt, 2, BMXG_FP64)
+    Q = w.particles.copy()
+    ctx.get_state(Q)
+    assert np.isfinite(Q["x"]).all()
+    ctx.set_stream(None)
