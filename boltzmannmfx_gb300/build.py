@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbmxg.so")
-SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "bmxg_ctx.cu"]
+SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "bmxg_ctx.cu", "bmxg_aos.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,7 +47,7 @@ def build(verbose=False, force=False, extra=()):
     jobs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(BUILD, s.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([cc, *flags(), *extra, "-c", src, "-o", obj])

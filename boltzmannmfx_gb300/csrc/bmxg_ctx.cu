@@ -95,6 +95,16 @@ int fail(bmxg_ctx *c, int code, const std::string &msg)
                         std::string(#call) + ": " + cudaGetErrorString(e_));                  \
     } while (0)
 
+// Enqueue a launcher (it returns how many kernels it launched), count them,
+// and turn a launch error into a status naming the launcher.
+#define LAUNCH(call)                                                                             \
+    do {                                                                                         \
+        ctx->launches += (call);                                                                 \
+        cudaError_t e_ = cudaPeekAtLastError();                                                  \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(ctx, BMXG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
 template <class T>
 int dalloc(bmxg_ctx *ctx, T **p, size_t count)
 {
@@ -299,6 +309,7 @@ int bmxg_set_stream(bmxg_ctx *ctx, void *stream)
 int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony_offsets, int where)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!p || p->n < 0 || !p->x || !p->y || !p->z || !p->radius || !p->cell_type)
         return fail(ctx, BMXG_ERR_ARG, "x, y, z, radius and cell_type are required");
     if (p->n > (1LL << 30)) return fail(ctx, BMXG_ERR_UNSUPPORTED, "more than 2^30 particles");
@@ -395,18 +406,18 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     CK(cudaMemcpyAsync(S.y[1], p->y, sizeof(double) * n, kind, st));
     CK(cudaMemcpyAsync(S.z[1], p->z, sizeof(double) * n, kind, st));
     // canonical order of the caller's particles
-    ctx->launches += launch_user_bin(S, S.x[1], S.y[1], S.z[1], S.col[1], S.iz[1], grd, blk, st);
-    ctx->launches += launch_scan(S.colcnt, S.colstart[1], (int)ncols, ctx->scan_scratch, st);
-    ctx->launches += launch_user_scatter_canon(S, S.col[1], S.iz[1], S.colstart[1], ctx->uperm, grd, blk, st);
+    LAUNCH(launch_user_bin(S, S.x[1], S.y[1], S.z[1], S.col[1], S.iz[1], grd, blk, st));
+    LAUNCH(launch_scan(S.colcnt, S.colstart[1], (int)ncols, ctx->scan_scratch, st));
+    LAUNCH(launch_user_scatter_canon(S, S.col[1], S.iz[1], S.colstart[1], ctx->uperm, grd, blk, st));
     CK(cudaMemcpyAsync(S.orig, ctx->uperm, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
     // gather every field into slot order
-    ctx->launches += launch_gather_d(S.x[0], S.x[1], ctx->uperm, (int)n, grd, blk, st);
-    ctx->launches += launch_gather_d(S.y[0], S.y[1], ctx->uperm, (int)n, grd, blk, st);
-    ctx->launches += launch_gather_d(S.z[0], S.z[1], ctx->uperm, (int)n, grd, blk, st);
+    LAUNCH(launch_gather_d(S.x[0], S.x[1], ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.y[0], S.y[1], ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.z[0], S.z[1], ctx->uperm, (int)n, grd, blk, st));
     auto up_d = [&](const double *src, double *dst, double fill) -> int {
         if (src) {
             CK(cudaMemcpyAsync(ctx->ud, src, sizeof(double) * n, kind, st));
-            ctx->launches += launch_gather_d(dst, ctx->ud, ctx->uperm, (int)n, grd, blk, st);
+            LAUNCH(launch_gather_d(dst, ctx->ud, ctx->uperm, (int)n, grd, blk, st));
         } else if (fill == 0.0) {
             CK(cudaMemsetAsync(dst, 0, sizeof(double) * n, st));
         } else {
@@ -420,7 +431,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     auto up_i = [&](const int32_t *src, int *dst, int planes, int fill) -> int {
         if (src) {
             CK(cudaMemcpyAsync(ctx->ui, src, sizeof(int) * n * planes, kind, st));
-            ctx->launches += launch_gather_i(dst, ctx->ui, ctx->uperm, (int)n, planes, grd, blk, st);
+            LAUNCH(launch_gather_i(dst, ctx->ui, ctx->uperm, (int)n, planes, grd, blk, st));
         } else {
             CK(cudaMemsetAsync(dst, fill == 0 ? 0 : 0xff, sizeof(int) * n * planes, st));
         }
@@ -428,7 +439,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     };
     if ((rc = up_d(p->radius, S.rad, 0.0))) return rc;
     CK(cudaMemcpyAsync(ctx->ui, p->cell_type, sizeof(int) * n, kind, st));
-    ctx->launches += launch_gather_i8(S.ctype, ctx->ui, ctx->uperm, (int)n, grd, blk, st);
+    LAUNCH(launch_gather_i8(S.ctype, ctx->ui, ctx->uperm, (int)n, grd, blk, st));
     if ((rc = up_d(p->velx, S.vx, 0.0))) return rc;
     if ((rc = up_d(p->vely, S.vy, 0.0))) return rc;
     if ((rc = up_d(p->velz, S.vz, 0.0))) return rc;
@@ -455,12 +466,12 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         if ((rc = up_i(p->seg_id1, S.tab[0] + n, 4, 0))) return rc;
         if ((rc = up_i(p->seg_id2, S.tab[0] + 5 * n, 4, 0))) return rc;
         if ((rc = up_i(p->site, S.tab[0] + 9 * n, 4, 0))) return rc;
-        ctx->launches += launch_trig(S, 0, grd, blk, st);
+        LAUNCH(launch_trig(S, 0, grd, blk, st));
     }
     // bins of the slots and the first column lists
     CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
-    ctx->launches += launch_bin(S, 0, grd, blk, st);
-    ctx->launches += launch_rebuild(S, 0, ctx->scan_scratch, grd, blk, st);
+    LAUNCH(launch_bin(S, 0, grd, blk, st));
+    LAUNCH(launch_rebuild(S, 0, ctx->scan_scratch, grd, blk, st));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->have_state = true;
@@ -474,6 +485,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
 int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (!p || p->n != ctx->n) return fail(ctx, BMXG_ERR_ARG, "particle count differs from the loaded state");
     if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
@@ -487,14 +499,14 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     const int a = ctx->parity;
     auto out_d = [&](double *dst, const double *src) -> int {
         if (!dst || !src) return BMXG_OK;
-        ctx->launches += launch_scatter_d(ctx->ud, src, S.orig, (int)n, grd, blk, st);
+        LAUNCH(launch_scatter_d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
         CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
         CK(cudaStreamSynchronize(st));
         return BMXG_OK;
     };
     auto out_i = [&](int32_t *dst, const int *src, int planes) -> int {
         if (!dst || !src) return BMXG_OK;
-        ctx->launches += launch_scatter_i(ctx->ui, src, S.orig, (int)n, planes, grd, blk, st);
+        LAUNCH(launch_scatter_i(ctx->ui, src, S.orig, (int)n, planes, grd, blk, st));
         CK(cudaMemcpyAsync(dst, ctx->ui, sizeof(int) * n * planes, kind, st));
         CK(cudaStreamSynchronize(st));
         return BMXG_OK;
@@ -539,7 +551,7 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
 namespace {
 
 // Enqueue one DEM step reading buffer a.
-void enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
+int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
 {
     const DevState &S = ctx->S;
     cudaStream_t st = ctx->stream;
@@ -567,17 +579,18 @@ void enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
     if (!S.has_rods) {
         const Shape &sh = ctx->sh_sphere[precision == BMXG_FP32F ? 1 : 0];
         if (k0) cudaEventRecord(k0, st);
-        ctx->launches += launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st);
+        LAUNCH(launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st));
         if (k1) cudaEventRecord(k1, st);
     } else {
         const int rg = grid_for(ctx, ctx->sh_rod, n);
-        ctx->launches += launch_rod_book(S, P, a, rg, ctx->sh_rod.block, st);
+        LAUNCH(launch_rod_book(S, P, a, rg, ctx->sh_rod.block, st));
         if (k0) cudaEventRecord(k0, st);
-        ctx->launches += launch_rod_force(S, P, a, precision, rg, ctx->sh_rod.block, st);
+        LAUNCH(launch_rod_force(S, P, a, precision, rg, ctx->sh_rod.block, st));
         if (k1) cudaEventRecord(k1, st);
-        ctx->launches += launch_rod_update(S, dt, a, mgrd, mblk, st);
+        LAUNCH(launch_rod_update(S, dt, a, mgrd, mblk, st));
     }
-    ctx->launches += launch_rebuild(S, b, ctx->scan_scratch, mgrd, mblk, st);
+    LAUNCH(launch_rebuild(S, b, ctx->scan_scratch, mgrd, mblk, st));
+    return BMXG_OK;
 }
 
 int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec_t *out)
@@ -591,9 +604,14 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
     cudaGraph_t g = nullptr;
     const int64_t before = ctx->launches;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(ctx, dt, precision, parity);
-    enqueue_step(ctx, dt, precision, parity ^ 1);
+    int rc1 = enqueue_step(ctx, dt, precision, parity);
+    int rc2 = rc1 ? rc1 : enqueue_step(ctx, dt, precision, parity ^ 1);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc2) {
+        if (g) cudaGraphDestroy(g);
+        ctx->launches = before;
+        return rc2;
+    }
     ctx->graph_kernels[key] = (int)(ctx->launches - before);  // counted per replay instead
     ctx->launches = before;
     if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -613,6 +631,7 @@ extern "C" {
 int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt or nsteps");
     if (precision != BMXG_FP64 && precision != BMXG_FP32F) return fail(ctx, BMXG_ERR_ARG, "bad precision");
@@ -635,7 +654,8 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
         }
     }
     while (left >= 1) {  // odd remainder, or every step in profiling mode
-        enqueue_step(ctx, subdt, precision, ctx->parity);
+        int rc = enqueue_step(ctx, subdt, precision, ctx->parity);
+        if (rc) return rc;
         ctx->parity ^= 1;
         --left;
     }
@@ -697,6 +717,7 @@ int bmxg_set_profiling(bmxg_ctx *ctx, int32_t on)
 int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int64_t cap, int64_t *total)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (!offs || !total) return fail(ctx, BMXG_ERR_ARG, "offs and total are required");
     const int64_t n = ctx->n;
@@ -748,6 +769,7 @@ int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int6
 int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (ctx->n == 0 || ctx->S.has_rods) return BMXG_OK;
     const int64_t n = ctx->n;
@@ -797,10 +819,10 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
                 s.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
                 const int grd = grid_for(ctx, s, n);
                 for (int w = 0; w < 2; ++w)
-                    ctx->launches += launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream);
+                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream));
                 CK(cudaEventRecord(ctx->ev0, ctx->stream));
                 for (int r = 0; r < 5; ++r)
-                    ctx->launches += launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream);
+                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream));
                 CK(cudaEventRecord(ctx->ev1, ctx->stream));
                 CK(cudaEventSynchronize(ctx->ev1));
                 float ms = 0.0f;

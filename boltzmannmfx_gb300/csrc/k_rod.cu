@@ -24,9 +24,10 @@
 //    :812-882).  The kernel therefore sums f1 + f2 and f1 - f2 over the pairs
 //    and applies the mobility once per segment: the same result up to
 //    rounding, without two 3x3 tensor rotations per pair.
-//  * FP32F: pair math in FP32 on the FP64-differenced bin-relative offsets;
-//    pairs whose segments are near-parallel (det < 0.05 Aii Ajj, where the
-//    closest-point solve loses precision) are solved in FP64.
+//  * FP32F: contact pair math in FP32 on the FP64-differenced bin-relative
+//    offsets; pairs whose segments are near-parallel (det < 0.05 Aii Ajj,
+//    where the closest-point solve loses precision) and bonded pairs (a
+//    spring on the difference of two coincident end points) are done in FP64.
 #include "bmxg_stencil.cuh"
 
 namespace bmxg {
@@ -336,10 +337,13 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                                            (me.z - q.z) - (float)dzs * G.dxf[2]};
                     const float nif[3] = {(float)ni[0], (float)ni[1], (float)ni[2]};
                     const float njf[3] = {(float)(trj.y * trj.z), (float)(trj.y * trj.w), (float)trj.x};
-                    // near-parallel test: det of the closest-point system
+                    // near-parallel test: det of the closest-point system.  Bonded
+                    // pairs stay FP64: their spring acts on the difference of two
+                    // coincident end points, which FP32 end points would swamp
+                    // with rounding noise (k_bond x ulp of the segment length).
                     const float rij = nif[0] * njf[0] + nif[1] * njf[1] + nif[2] * njf[2];
                     const bool bonded = (si == 1 || si == 2) && (sj == 1 || sj == 2);
-                    if (bonded || 1.0f - rij * rij >= 0.05f) {
+                    if (!bonded && 1.0f - rij * rij >= 0.05f) {
                         float g1[3], g2[3];
                         rod_site_forces<float>(r12f, nif, (float)Li, njf, (float)Lj, (float)rS, (float)rA,
                                                (float)P.k, si, sj, (float)kb, g1, g2);

@@ -22,8 +22,8 @@ _lib = None
 # every entry point include/bmxg.h declares
 ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy", "bmxg_set_params",
                "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
-               "bmxg_evolve_particles", "bmxg_get_stats", "bmxg_set_profiling", "bmxg_get_pairs",
-               "bmxg_autotune")
+               "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
+               "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_autotune")
 
 
 class BmxgError(RuntimeError):
@@ -54,6 +54,9 @@ def load_library(path=None):
     L.bmxg_get_state.argtypes = [vp, C.POINTER(ParticlesStruct), C.c_int]
     L.bmxg_step.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
     L.bmxg_evolve_particles.argtypes = [vp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+    L.bmxg_evolve_particles_aos.argtypes = [vp, vp, C.c_int64, C.c_int32, C.c_int32,
+                                            C.POINTER(C.c_int64), C.c_double, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_int32)]
     L.bmxg_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.bmxg_set_profiling.argtypes = [vp, C.c_int32]
     L.bmxg_get_pairs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int8),

@@ -191,6 +191,19 @@ int  bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision);
 int  bmxg_evolve_particles(bmxg_ctx *ctx, double dt, double *cost_per_colony,
                            int32_t *nsubsteps);
 
+/* The same step on particles kept in the reference's own layout:
+ * amrex::Particle<nreal, nint> of AMReX 22.x in double precision, i.e.
+ * double pos[3]; double rdata[nreal]; int id, cpu; int idata[nint]
+ * (448-byte structs for BMX's 34 / 35, src/chemistry/bmx_chem.H:16-17), in
+ * host memory.  Loads them, runs one step (bmxg_evolve_particles) and writes
+ * back what EvolveParticles writes: pos, velx..velz, wx..wz, theta, phi and
+ * the integer fields its pair loop and wall force change
+ * (bmx_pc_interaction.cpp:174-279, :317-436).  nreal >= 25, nint >= 35. */
+int  bmxg_evolve_particles_aos(bmxg_ctx *ctx, void *particles, int64_t n,
+                               int32_t nreal, int32_t nint,
+                               const int64_t *colony_offsets, double dt,
+                               double *cost_per_colony, int32_t *nsubsteps);
+
 int  bmxg_get_stats(const bmxg_ctx *ctx, bmxg_stats *out);
 
 /* Profiling mode: when on, bmxg_step launches eagerly (no graph) and times

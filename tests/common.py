@@ -52,3 +52,30 @@ def mirror(img):
     sx = img % 3 - 1
     sy = img // 3 - 1
     return (1 - sx) + 3 * (1 - sy)
+
+
+def trig_floor(O, prm, geom, P):
+    """How far the reference step's velocity (rows 0-2) and angular velocity
+    (rows 3-5) move when every segment's angles move by one ulp -- the size
+    of a last-bit difference between two libm sin/cos implementations.
+    Bonded rod ends coincide, so bond forces are k_bond times the rounding
+    noise of the end-point arithmetic; two correct implementations with
+    different sin/cos disagree at this level.  Returns (floor_v, floor_w)."""
+    pl = O.pairs(prm, geom, P)
+    base = P.copy()
+    fc0 = O.forces(prm, geom, base, pl)
+    dv = np.zeros(6)
+    for direction in (np.inf, -np.inf):
+        Q = P.copy()
+        Q["theta"] = np.nextafter(Q["theta"], direction)
+        Q["phi"] = np.nextafter(Q["phi"], direction)
+        fc = O.forces(prm, geom, Q, pl)
+        dv = np.maximum(dv, np.abs(fc - fc0).max(axis=1))
+    return float(dv[:3].max()), float(dv[3:].max())
+
+
+def within(a, b, rel, floor):
+    """max |a - b| <= rel * max |b| + floor"""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max()) <= rel * float(np.abs(b).max()) + floor

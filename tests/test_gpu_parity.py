@@ -13,7 +13,7 @@ import pytest
 
 from boltzmannmfx_gb300 import Context, configs
 from boltzmannmfx_gb300.abi import BMXG_FP32F, BMXG_FP64, Particles
-from common import geom_of, load, params_of, particles_of, relerr, same_pairs
+from common import geom_of, load, params_of, particles_of, relerr, same_pairs, trig_floor, within
 
 pytestmark = pytest.mark.gpu
 
@@ -66,15 +66,21 @@ def test_sphere_fp64_bitexact_golden(gpu_lib, case):
 
 
 @pytest.mark.parametrize("case", ["rods_small", "mixed", "half_bond", "wall_test"])
-def test_rod_fp64_golden(gpu_lib, case):
+def test_rod_fp64_golden(gpu_lib, oracle_lib, case):
+    """Within 1e-10 of the field's scale, plus the reference's own sensitivity
+    to a one-ulp change of the segment angles (trig_floor): CUDA's and glibc's
+    sin/cos may differ in the last bit, and bond forces on coincident ends
+    are k_bond times end-point rounding noise."""
     d = load(case)
     P = particles_of(d)
-    ctx = gpu_ctx(params_of(d), [geom_of(d)], P)
+    prm, g = params_of(d), geom_of(d)
+    fv, fw = trig_floor(oracle_lib, prm, g, P)
+    ctx = gpu_ctx(prm, [g], P)
     ctx.step(float(d["dt"]), 1, BMXG_FP64)
     Q = readback(ctx, P)
     fc = np.stack([Q[k] for k in ("velx", "vely", "velz", "wx", "wy", "wz")])
-    assert relerr(fc[:3], d["fc1"][:3]) <= TOL64
-    assert relerr(fc[3:], d["fc1"][3:]) <= TOL64
+    assert within(fc[:3], d["fc1"][:3], TOL64, 8 * fv)
+    assert within(fc[3:], d["fc1"][3:], TOL64, 8 * fw)
     for k in ("x", "y", "z", "theta", "phi"):
         assert relerr(Q[k], d["s1_" + k]) <= TOL64, k
     for k in INT_FIELDS:

@@ -190,3 +190,16 @@ def test_wall_equilibrium(oracle_lib):
         v, _ = oracle_lib.surface_force(prm, P, 0)
         scale = prm.z_stiffness * (6e-4 + prm.z_bndry_width) ** 2 * 6e-4
         assert (abs(v[2]) < 1e-12 * scale) == zero
+
+
+def test_rod_noise_floor_is_real(oracle_lib):
+    """A one-ulp change of the segment angles moves the reference's rod
+    velocities by more than 1e-10 of their scale: coincident bonded ends make
+    the bond force k_bond x rounding noise.  This is why the FP64 rod bar
+    adds that sensitivity to the 1e-10 relative tolerance."""
+    from common import trig_floor
+    d = load("rods_small")
+    fv, fw = trig_floor(oracle_lib, params_of(d), geom_of(d), particles_of(d))
+    vmax = np.abs(d["fc1"][:3]).max()
+    assert fv > 1e-11 * vmax
+    assert fv < 1e-6 * vmax
