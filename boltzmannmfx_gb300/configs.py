@@ -25,6 +25,7 @@ from .abi import SITE_INTERIOR, SITE_SECOND_2, SITE_TIP
 BIN = 0.002            # cm, level-2 cell of the fungi deck
 Z_BAND = (0.040, 0.052)  # bmx.tag_region_lo/hi z of exec/fungi/input_fungi:46-47
 SEED = 43343           # bmx.seed of exec/fungi/input_fungi:5
+ROD_DT = 2.5e-4        # stable step for k_bond = 5e3 (see rod_trees)
 
 
 def deck_params(stiffness=1.0e3, bond_strength=5.0e3):
@@ -210,8 +211,14 @@ def rod_trees(seed=SEED, ntrees=500, per_tree=100, lx=0.512, ly=0.512,
         if has_child[i] and any((not has_child[j]) and site == 2 for j, site in bonds[i]):
             pos[i] = SITE_SECOND_2
     P["position"] = pos
+    # The configuration names k_bond = 5e3 but no time step.  The explicit
+    # overdamped update is stable for a bond only while
+    # dt * k_bond * (d0 + db) < 2 (closing rate of two bonded ends, segment
+    # mobility d0 + db ~ 0.9 at viscous_drag = 200); the plain-form
+    # dt = 0.25 breaks that 400-fold and the reference trajectory leaves the
+    # box within a few steps.  dt = 2.5e-4 keeps k_bond = 5e3 inside the bound.
     return Workload("rod_trees_50k" if n == 50_000 else f"rod_trees_{n}", deck_params(),
-                    [box_geometry(lx, ly)], P, np.array([0, n], np.int64), 0.25, 200, 0)
+                    [box_geometry(lx, ly)], P, np.array([0, n], np.int64), ROD_DT, 200, 0)
 
 
 def by_name(name, **kw):

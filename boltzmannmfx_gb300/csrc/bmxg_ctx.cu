@@ -811,7 +811,7 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
         const DevParams P = dev_params(ctx->prm);
         float best = 1e30f;
         Shape bs = ctx->sh_sphere[prec];
-        const int blocks[] = {64, 128, 256, 512};
+        const int blocks[] = {64, 128, 256};  // k_sphere is compiled with __launch_bounds__(256)
         for (int blk : blocks) {
             for (int mult = 1; mult <= 16; mult *= 2) {
                 Shape s;

@@ -9,7 +9,8 @@ them in the reference, is not in the reference tree).
 
 Cases:
   sphere_plain   2 000 spheres of the plain-form configuration, 1 and 20 steps
-  rods_small     400 rod segments in 10 branching trees, 1 and 20 steps
+  rods_small     400 rod segments in 10 branching trees, 1 and 20 steps (rod
+                 cases use the stable rod step configs.ROD_DT)
   mixed          spheres and rods in one state
   half_bond      rods with a one-sided bond and a SECOND_2 segment (bookkeeping)
   pair_test      the two spheres across the periodic x face of exec/pair_test
@@ -124,7 +125,7 @@ def mixed():
     S["id"] = np.arange(R.n + 1, R.n + S.n + 1, dtype=np.int32)
     P = Particles.concat([R, S])
     P.rods = True
-    run_case("mixed", w.params, configs.box_geometry(0.032, 0.032), P, 0.25, 10)
+    run_case("mixed", w.params, configs.box_geometry(0.032, 0.032), P, configs.ROD_DT, 10)
 
 
 def half_bond():
@@ -141,7 +142,7 @@ def half_bond():
         s1[nb[i], i] = 0
     P["fix_site"][cut[0]] = 2
     P["position"][cut[1]] = 1
-    run_case("half_bond", w.params, w.geoms[0], P, 0.25, 3)
+    run_case("half_bond", w.params, w.geoms[0], P, configs.ROD_DT, 3)
 
 
 def pair_test():

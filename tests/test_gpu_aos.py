@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from boltzmannmfx_gb300 import Context
-from common import geom_of, load, params_of, particles_of, relerr
+from common import geom_of, load, params_of, particles_of, relerr, trig_floor, within
 
 pytestmark = pytest.mark.gpu
 
@@ -39,9 +39,10 @@ def to_aos(P):
 
 
 @pytest.mark.parametrize("case", ["sphere_plain", "rods_small"])
-def test_aos_entry_matches_golden(gpu_lib, case):
+def test_aos_entry_matches_golden(gpu_lib, oracle_lib, case):
     d = load(case)
     P = particles_of(d)
+    fv, fw = trig_floor(oracle_lib, params_of(d), geom_of(d), P) if case != "sphere_plain" else (0.0, 0.0)
     ctx = Context(params_of(d), [geom_of(d)])
     a = to_aos(P)
     cost = (C.c_double * 1)()
@@ -53,7 +54,11 @@ def test_aos_entry_matches_golden(gpu_lib, case):
     tol = 0.0 if case == "sphere_plain" else 1e-10
     for k, col in (("x", 0), ("y", 1), ("z", 2)):
         assert relerr(a["pos"][:, col], d["s1_" + k]) <= tol, k
-    for k in ("velx", "vely", "velz", "wx", "wy", "wz", "theta", "phi"):
+    for k, floor in (("velx", fv), ("vely", fv), ("velz", fv), ("wx", fw), ("wy", fw), ("wz", fw)):
+        ref = d["fc1"][["velx", "vely", "velz", "wx", "wy", "wz"].index(k)]
+        scale = np.abs(d["fc1"][:3] if k.startswith("vel") else d["fc1"][3:]).max()
+        assert np.abs(a["rdata"][:, R[k]] - ref).max() <= tol * scale + 8 * floor, k
+    for k in ("theta", "phi"):
         assert relerr(a["rdata"][:, R[k]], d["s1_" + k]) <= tol, k
     for k in ("n_bnds", "position", "fix_site", "fuse_flag"):
         assert np.array_equal(a["idata"][:, I[k]], d["s1_" + k]), k
