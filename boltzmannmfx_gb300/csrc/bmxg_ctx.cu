@@ -77,6 +77,18 @@ struct bmxg_ctx {
     bool profiling = false;
     std::vector<cudaEvent_t> kev;           // event pairs around the force kernel, profiling mode
     size_t kev_used = 0;
+
+    // differentiation form
+    double ext_gamma = 0.0, ext_mu = 0.0;
+    double *d_adh = nullptr;                // per-slot adhesion in use (nullptr: zero)
+    double *adh_buf = nullptr;              // its buffer, allocated with the state
+    std::vector<void *> dallocs;            // adjoint buffers (freed with the state)
+    double *ckpt = nullptr;                 // (nseg + 1) x 3n positions, slot order
+    double *segbuf = nullptr;               // ckpt_every x 3n positions of one segment
+    double *lam[2] = {nullptr, nullptr};    // adjoint of the positions, 3 planes
+    double *gacc = nullptr, *gadh = nullptr, *gout = nullptr, *xT = nullptr;
+    int traj_T = -1, traj_k = 0;
+    double traj_dt = 0.0;
 };
 
 namespace {
@@ -123,9 +135,20 @@ void drop_graphs(bmxg_ctx *ctx)
     ctx->graph_kernels.clear();
 }
 
+void free_adjoint(bmxg_ctx *ctx)
+{
+    for (void *p : ctx->dallocs) cudaFree(p);
+    ctx->dallocs.clear();
+    ctx->ckpt = ctx->segbuf = ctx->gacc = ctx->gadh = ctx->gout = ctx->xT = nullptr;
+    ctx->lam[0] = ctx->lam[1] = nullptr;
+    ctx->traj_T = -1;
+}
+
 void free_state(bmxg_ctx *ctx)
 {
     drop_graphs(ctx);
+    free_adjoint(ctx);
+    ctx->d_adh = ctx->adh_buf = nullptr;  // lives in allocs
     for (void *p : ctx->allocs) cudaFree(p);
     ctx->allocs.clear();
     ctx->S = DevState{};
@@ -477,6 +500,8 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     ctx->have_state = true;
     ctx->stepped = false;
     ctx->parity = 0;
+    ctx->d_adh = nullptr;  // per-particle adhesion must be given again for the new state
+    free_adjoint(ctx);
     std::memset(&ctx->stats, 0, sizeof(ctx->stats));
     ctx->stats.n_particles = n;
     return BMXG_OK;
@@ -862,6 +887,226 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
         }
     }
     drop_graphs(ctx);
+    return BMXG_OK;
+}
+
+}  // extern "C"
+
+// ---- differentiation form ----------------------------------------------------
+extern "C" {
+
+int bmxg_set_ext(bmxg_ctx *ctx, const bmxg_ext *ext)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ext || !std::isfinite(ext->damping) || !std::isfinite(ext->mu) || ext->damping < 0.0 || ext->mu < 0.0)
+        return fail(ctx, BMXG_ERR_ARG, "damping and mu must be finite and >= 0");
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "load the state before its extension parameters");
+    (void)cudaGetLastError();
+    ctx->ext_gamma = ext->damping;
+    ctx->ext_mu = ext->mu;
+    const int64_t n = ctx->n;
+    if (ext->adhesion && n > 0) {
+        if (!ctx->adh_buf) {
+            int rc = dalloc(ctx, &ctx->adh_buf, n);
+            if (rc) return rc;
+        }
+        ctx->d_adh = ctx->adh_buf;
+        cudaStream_t st = ctx->stream;
+        CK(cudaMemcpyAsync(ctx->ud, ext->adhesion, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        LAUNCH(launch_gather_d(ctx->d_adh, ctx->ud, ctx->S.orig, (int)n, grid_for(ctx, ctx->sh_misc, n),
+                               ctx->sh_misc.block, st));
+        CK(cudaStreamSynchronize(st));
+    } else {
+        ctx->d_adh = nullptr;  // buffer (if any) stays allocated until the state is freed
+    }
+    ctx->traj_T = -1;
+    return BMXG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+int dalloc_adj(bmxg_ctx *ctx, T **p, size_t count)
+{
+    void *q = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(&q, count * sizeof(T)));
+    ctx->dallocs.push_back(q);
+    *p = (T *)q;
+    return BMXG_OK;
+}
+
+DiffParams diff_params(const bmxg_ctx *ctx)
+{
+    return DiffParams{ctx->ext_gamma, ctx->ext_mu, ctx->d_adh};
+}
+
+// copy the positions of buffer b into 3 planes at dst (slot order)
+int save_pos(bmxg_ctx *ctx, int b, double *dst)
+{
+    const size_t bytes = sizeof(double) * ctx->n;
+    CK(cudaMemcpyAsync(dst, ctx->S.x[b], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dst + ctx->n, ctx->S.y[b], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dst + 2 * ctx->n, ctx->S.z[b], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return BMXG_OK;
+}
+
+// load 3 position planes into buffer 0 and rebuild its bins and column lists
+int load_pos(bmxg_ctx *ctx, const double *src)
+{
+    const size_t bytes = sizeof(double) * ctx->n;
+    const DevState &S = ctx->S;
+    CK(cudaMemcpyAsync(S.x[0], src, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.y[0], src + ctx->n, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.z[0], src + 2 * ctx->n, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, ctx->n);
+    LAUNCH(launch_bin(S, 0, mgrd, mblk, ctx->stream));
+    LAUNCH(launch_rebuild(S, 0, ctx->scan_scratch, mgrd, mblk, ctx->stream));
+    ctx->parity = 0;
+    return BMXG_OK;
+}
+
+int dfwd_step(bmxg_ctx *ctx, double dt)
+{
+    const DevState &S = ctx->S;
+    const int a = ctx->parity;
+    const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, ctx->n);
+    const Shape &sh = ctx->sh_sphere[0];
+    LAUNCH(launch_dfwd(S, dev_params(ctx->prm), diff_params(ctx), dt, a, grid_for(ctx, sh, ctx->n), sh.block,
+                       ctx->stream));
+    LAUNCH(launch_rebuild(S, a ^ 1, ctx->scan_scratch, mgrd, mblk, ctx->stream));
+    ctx->parity = a ^ 1;
+    return BMXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (ctx->S.has_rods) return fail(ctx, BMXG_ERR_UNSUPPORTED, "the differentiation form covers spheres");
+    if (nsteps < 0 || ckpt_every < 1 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt, nsteps or ckpt_every");
+    (void)cudaGetLastError();
+    const int64_t n = ctx->n;
+    free_adjoint(ctx);
+    if (n == 0) {
+        ctx->traj_T = nsteps;
+        ctx->traj_k = ckpt_every;
+        ctx->traj_dt = dt;
+        return BMXG_OK;
+    }
+    const int nseg = (nsteps + ckpt_every - 1) / ckpt_every;
+    int rc;
+    if ((rc = dalloc_adj(ctx, &ctx->ckpt, (size_t)(nseg + 1) * 3 * n))) return rc;
+    if ((rc = dalloc_adj(ctx, &ctx->xT, (size_t)3 * n))) return rc;
+    const double subdt = dt / 1.0;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (int t = 0; t < nsteps; ++t) {
+        if (t % ckpt_every == 0 && (rc = save_pos(ctx, ctx->parity, ctx->ckpt + (size_t)(t / ckpt_every) * 3 * n)))
+            return rc;
+        if ((rc = dfwd_step(ctx, subdt))) return rc;
+    }
+    if ((rc = save_pos(ctx, ctx->parity, ctx->xT))) return rc;
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.last_step_ms = ms;
+    ctx->stepped = true;
+    ctx->traj_T = nsteps;
+    ctx->traj_k = ckpt_every;
+    ctx->traj_dt = subdt;
+    ctx->stats.n_kernel_launches = ctx->launches;
+    if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
+    return BMXG_OK;
+}
+
+int bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0, double *dL_dparams, double *dL_dadhesion)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (ctx->traj_T < 0) return fail(ctx, BMXG_ERR_STATE, "bmxg_forward must run first");
+    if (!dL_dx) return fail(ctx, BMXG_ERR_ARG, "dL_dx is required");
+    (void)cudaGetLastError();
+    const int64_t n = ctx->n;
+    const int T = ctx->traj_T, K = ctx->traj_k;
+    if (n == 0) {
+        if (dL_dparams) dL_dparams[0] = dL_dparams[1] = dL_dparams[2] = 0.0;
+        return BMXG_OK;
+    }
+    cudaStream_t st = ctx->stream;
+    const DevState &S = ctx->S;
+    int rc;
+    if (!ctx->lam[0]) {
+        if ((rc = dalloc_adj(ctx, &ctx->lam[0], (size_t)3 * n))) return rc;
+        if ((rc = dalloc_adj(ctx, &ctx->lam[1], (size_t)3 * n))) return rc;
+        if ((rc = dalloc_adj(ctx, &ctx->segbuf, (size_t)K * 3 * n))) return rc;
+        if ((rc = dalloc_adj(ctx, &ctx->gacc, (size_t)3 * n))) return rc;
+        if ((rc = dalloc_adj(ctx, &ctx->gadh, (size_t)n))) return rc;
+        if ((rc = dalloc_adj(ctx, &ctx->gout, 4))) return rc;
+    }
+    const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
+    CK(cudaEventRecord(ctx->ev0, st));
+    // dL/dx_T, caller order -> slot order
+    for (int c = 0; c < 3; ++c) {
+        CK(cudaMemcpyAsync(ctx->ud, dL_dx + (size_t)c * n, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        LAUNCH(launch_gather_d(ctx->lam[0] + (size_t)c * n, ctx->ud, S.orig, (int)n, mgrd, mblk, st));
+    }
+    CK(cudaMemsetAsync(ctx->gacc, 0, sizeof(double) * 3 * n, st));
+    CK(cudaMemsetAsync(ctx->gadh, 0, sizeof(double) * n, st));
+    int cur = 0;
+    const DevParams P = dev_params(ctx->prm);
+    const DiffParams D = diff_params(ctx);
+    const Shape &sh = ctx->sh_sphere[0];
+    const int nseg = (T + K - 1) / K;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int c0 = seg * K, c1 = std::min(c0 + K, T);
+        // recompute the segment's positions from its checkpoint
+        if ((rc = load_pos(ctx, ctx->ckpt + (size_t)seg * 3 * n))) return rc;
+        for (int t = c0; t < c1; ++t) {
+            if ((rc = save_pos(ctx, ctx->parity, ctx->segbuf + (size_t)(t - c0) * 3 * n))) return rc;
+            if (t + 1 < c1 && (rc = dfwd_step(ctx, ctx->traj_dt))) return rc;
+        }
+        // reverse sweep through the segment
+        for (int t = c1 - 1; t >= c0; --t) {
+            if ((rc = load_pos(ctx, ctx->segbuf + (size_t)(t - c0) * 3 * n))) return rc;
+            LAUNCH(launch_dadj(S, P, D, ctx->traj_dt, 0, ctx->lam[cur], ctx->lam[cur ^ 1], ctx->gacc, ctx->gadh,
+                               grid_for(ctx, sh, n), sh.block, st));
+            cur ^= 1;
+        }
+    }
+    LAUNCH(launch_dreduce(ctx->gacc, (int)n, 3, ctx->gout, st));
+    CK(cudaEventRecord(ctx->ev1, st));
+    if (dL_dx0) {
+        for (int c = 0; c < 3; ++c) {
+            LAUNCH(launch_scatter_d(ctx->ud, ctx->lam[cur] + (size_t)c * n, S.orig, (int)n, mgrd, mblk, st));
+            CK(cudaMemcpyAsync(dL_dx0 + (size_t)c * n, ctx->ud, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    }
+    if (dL_dadhesion) {
+        LAUNCH(launch_scatter_d(ctx->ud, ctx->gadh, S.orig, (int)n, mgrd, mblk, st));
+        CK(cudaMemcpyAsync(dL_dadhesion, ctx->ud, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    }
+    double g[3] = {0.0, 0.0, 0.0};
+    CK(cudaMemcpyAsync(g, ctx->gout, sizeof(g), cudaMemcpyDeviceToHost, st));
+    // leave the state at the end of the trajectory, as bmxg_forward did
+    if ((rc = load_pos(ctx, ctx->xT))) return rc;
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.last_step_ms = ms;
+    ctx->stats.n_kernel_launches = ctx->launches;
+    if (dL_dparams) {
+        dL_dparams[0] = g[0];
+        dL_dparams[1] = g[1];
+        dL_dparams[2] = ctx->ext_mu > 0.0 ? g[2] : 0.0;
+    }
     return BMXG_OK;
 }
 

@@ -44,6 +44,13 @@ struct DevState {
     double *fc;        // 6 planes, force gather of the rod path
 };
 
+// Extension parameters of the differentiation form (k_adjoint.cu).
+struct DiffParams {
+    double gamma;        // two-body dashpot
+    double mu;           // Stokes drag of spheres (0: mobility 1)
+    const double *adh;   // per-slot adhesion energy (null: zero)
+};
+
 // ---- binning / counting sort (k_bin.cu) ----------------------------------
 int launch_bin(const DevState &S, int b, int grid, int block, cudaStream_t st);
 int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st);
@@ -78,5 +85,12 @@ int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int 
 int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
                       cudaStream_t st);
 int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st);
+
+// ---- differentiation form (k_adjoint.cu) ---------------------------------
+int launch_dfwd(const DevState &S, const DevParams &P, const DiffParams &D, double dt, int a, int grid, int block,
+                cudaStream_t st);
+int launch_dadj(const DevState &S, const DevParams &P, const DiffParams &D, double dt, int a, const double *lin,
+                double *lout, double *gacc, double *gadh, int grid, int block, cudaStream_t st);
+int launch_dreduce(const double *gacc, int n, int planes, double *out, cudaStream_t st);
 
 }  // namespace bmxg

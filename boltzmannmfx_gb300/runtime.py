@@ -23,7 +23,13 @@ _lib = None
 ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy", "bmxg_set_params",
                "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
-               "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_autotune")
+               "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
+               "bmxg_backward", "bmxg_autotune")
+
+
+class Ext(C.Structure):
+    """bmxg_ext: extension parameters of the differentiation form."""
+    _fields_ = [("damping", C.c_double), ("mu", C.c_double), ("adhesion", C.POINTER(C.c_double))]
 
 
 class BmxgError(RuntimeError):
@@ -62,6 +68,10 @@ def load_library(path=None):
     L.bmxg_get_pairs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int8),
                                  C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
+    L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
+    L.bmxg_forward.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
+    L.bmxg_backward.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]
     if path is None:
         _lib = L
     return L
@@ -159,6 +169,30 @@ class Context:
                                             idx.ctypes.data_as(C.POINTER(C.c_int32)),
                                             img.ctypes.data_as(C.POINTER(C.c_int8)), cap, C.byref(total)))
         return offs, idx[:total.value], img[:total.value]
+
+    def set_ext(self, damping=0.0, mu=0.0, adhesion=None):
+        e = Ext()
+        e.damping = damping
+        e.mu = mu
+        self._adh = None if adhesion is None else np.ascontiguousarray(adhesion, np.float64)
+        e.adhesion = (self._adh.ctypes.data_as(C.POINTER(C.c_double)) if self._adh is not None
+                      else C.POINTER(C.c_double)())
+        self._check(self.lib.bmxg_set_ext(self.h, C.byref(e)))
+
+    def forward(self, dt, nsteps, ckpt_every=20):
+        self._check(self.lib.bmxg_forward(self.h, dt, nsteps, ckpt_every))
+
+    def backward(self, dL_dx):
+        """dL_dx: (3, n) gradient w.r.t. the final positions.  Returns
+        (dL/dx0 (3, n), dL/d(stiffness, damping, mu) (3,), dL/dadhesion (n,))."""
+        g = np.ascontiguousarray(dL_dx, np.float64).reshape(-1)
+        gx0 = np.zeros(3 * self.n)
+        gp = np.zeros(3)
+        ga = np.zeros(self.n)
+        dp = C.POINTER(C.c_double)
+        self._check(self.lib.bmxg_backward(self.h, g.ctypes.data_as(dp), gx0.ctypes.data_as(dp),
+                                           gp.ctypes.data_as(dp), ga.ctypes.data_as(dp)))
+        return gx0.reshape(3, self.n), gp, ga
 
     def autotune(self, cache_path=None):
         self._check(self.lib.bmxg_autotune(self.h, cache_path.encode() if cache_path else None))

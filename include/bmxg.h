@@ -224,6 +224,37 @@ int  bmxg_set_profiling(bmxg_ctx *ctx, int32_t on);
 int  bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img,
                     int64_t cap, int64_t *total);
 
+/* ---- differentiation form ------------------------------------------------ */
+
+/* Contact-parameter extensions of the sphere law used by the differentiable
+ * step (all zero: the reference law, bit for bit):
+ *   damping   gamma of a two-body overdamped dashpot, F -> F / (1 + gamma (m_i + m_j))
+ *   mu        Stokes drag: pair forces move sphere i with mobility
+ *             m_i = 1 / (6 pi mu r_i) instead of 1 (the reference folds drag into k)
+ *   adhesion  per-particle adhesion energy a_i (caller order, NULL = 0) in units
+ *             of the band's spring energy: F -= k bw (a_i + a_j)/2 (r - rA)^2
+ * Set after bmxg_set_state (the adhesion array follows the loaded state). */
+typedef struct bmxg_ext {
+    double damping;
+    double mu;
+    const double *adhesion;
+} bmxg_ext;
+int  bmxg_set_ext(bmxg_ctx *ctx, const bmxg_ext *ext);
+
+/* Differentiable FP64 trajectory of nsteps spheres steps from the loaded
+ * state (the loaded state then holds the final positions), keeping a
+ * checkpoint of the positions every ckpt_every steps. */
+int  bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every);
+
+/* Hand-written adjoint of that trajectory.  dL_dx: [3][n] gradient of a loss
+ * with respect to the final positions (x plane, y plane, z plane; caller
+ * order).  Out (each may be NULL): dL_dx0 [3][n] gradient with respect to the
+ * initial positions, dL_dparams[3] = dL/d(stiffness, damping, mu),
+ * dL_dadhesion [n].  Segments between checkpoints are recomputed forward and
+ * swept backward; the neighbour lists are the ones the forward step built. */
+int  bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0,
+                   double *dL_dparams, double *dL_dadhesion);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* Time the launch shapes of the step kernels on the loaded state and keep
