@@ -24,7 +24,7 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
                "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
-               "bmxg_backward", "bmxg_autotune")
+               "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_autotune")
 
 
 class Ext(C.Structure):
@@ -69,6 +69,8 @@ def load_library(path=None):
                                  C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
+    L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
+        [C.c_double, vp]
     L.bmxg_forward.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
     L.bmxg_backward.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_double)]

@@ -255,6 +255,34 @@ int  bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every);
 int  bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0,
                    double *dL_dparams, double *dL_dadhesion);
 
+/* ---- a step that allocates nothing ---------------------------------------- */
+
+/* One FP64 step of a sphere colony on caller-owned DEVICE arrays, without
+ * any device allocation.  This entry point has no counterpart in the
+ * reference; it exists for callers that may not call cudaMalloc on the
+ * step's path -- an application that hands out all device memory through
+ * its own arenas (as AMReX does), or a host program recording the step
+ * into someone else's stream capture, where allocation is not allowed.
+ * Inputs x, y, z, radius (n each) and outputs x_out, y_out, z_out and
+ * vel_x..vel_z (n each; may not alias the inputs) are device pointers in
+ * the caller's order; all particles are spheres of one colony with geometry
+ * `geom`.  The result equals bmxg_set_state + bmxg_step(dt, 1, BMXG_FP64) +
+ * bmxg_get_state bit for bit.
+ * Limits: n <= 32768 and n_cell[0] * n_cell[1] <= 65536, else
+ * BMXG_ERR_CAPACITY.  The binning scratch is one fixed device array of about
+ * 2.3 MB that every GPU loading the library holds until the process exits.
+ * The first call on a device looks up that array's address (make it before
+ * any stream capture).  Every call reuses the array: calls that overlap on
+ * the GPU (other streams, other host threads) race and must not be issued.
+ * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ * returns after it completes. */
+int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *geom,
+                              int64_t n, const double *x, const double *y,
+                              const double *z, const double *radius,
+                              double *x_out, double *y_out, double *z_out,
+                              double *vel_x, double *vel_y, double *vel_z,
+                              double dt, void *stream);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* Time the launch shapes of the step kernels on the loaded state and keep
