@@ -89,6 +89,9 @@ struct bmxg_ctx {
     double *gacc = nullptr, *gadh = nullptr, *gout = nullptr, *xT = nullptr;
     int traj_T = -1, traj_k = 0;
     double traj_dt = 0.0;
+
+    bool vel32 = false;       // the last step's velocities are in the FP32F buffers
+    int64_t step_count = 0;   // steps since set_state (FP32F re-sync schedule)
 };
 
 namespace {
@@ -235,6 +238,16 @@ void build_geoms(bmxg_ctx *ctx)
         G.slot_end = (int)ctx->offsets[c + 1];
         // two bins apart at most per axis: |r|^2 < 4 (dx^2 + dy^2 + dz^2)
         G.nbh_trivial = (ctx->prm.neighborhood >= diag2 * (1.0 + 1e-9)) ? 1 : 0;
+        G.invny = 1.0f / (float)G.n[1];
+        // height of each z-bin's lower face above the growth surface, with the
+        // same FP64 face the re-binning uses, split into a float pair
+        G.nwz = std::min(G.n[2] + 2, kWallTable);
+        for (int bz = 0; bz < G.nwz; ++bz) {
+            const double face = G.plo[2] + (double)(bz - 1) * G.dx[2];
+            const double h = face - ctx->prm.z_wall;
+            const float hi = (float)h;
+            G.wz[bz] = make_float2(hi, (float)(h - (double)hi));
+        }
     }
 }
 
@@ -398,6 +411,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     AL(S.colcnt, ncols); AL(S.tmp, n);
     AL(S.rad, n); AL(S.orig, n); AL(S.ctype, n);
     AL(S.vx, n); AL(S.vy, n); AL(S.vz, n); AL(S.wx, n); AL(S.wy, n); AL(S.wz, n);
+    AL(S.vxf, n); AL(S.vyf, n); AL(S.vzf, n);
     AL(ctx->scan_scratch, scan_scratch_ints((int)ncols));
     AL(ctx->ud, n); AL(ctx->ui, 13 * n + 1); AL(ctx->uperm, n);
     if (rods) {
@@ -499,6 +513,8 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     CK(cudaStreamSynchronize(st));
     ctx->have_state = true;
     ctx->stepped = false;
+    ctx->vel32 = false;
+    ctx->step_count = 0;
     ctx->parity = 0;
     ctx->d_adh = nullptr;  // per-particle adhesion must be given again for the new state
     free_adjoint(ctx);
@@ -536,13 +552,26 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
         CK(cudaStreamSynchronize(st));
         return BMXG_OK;
     };
+    auto out_f = [&](double *dst, const float *src) -> int {  // FP32F velocities, widened
+        if (!dst || !src) return BMXG_OK;
+        LAUNCH(launch_scatter_f2d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
+        CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
+        CK(cudaStreamSynchronize(st));
+        return BMXG_OK;
+    };
     int rc;
     if ((rc = out_d(p->x, S.x[a]))) return rc;
     if ((rc = out_d(p->y, S.y[a]))) return rc;
     if ((rc = out_d(p->z, S.z[a]))) return rc;
-    if ((rc = out_d(p->velx, S.vx))) return rc;
-    if ((rc = out_d(p->vely, S.vy))) return rc;
-    if ((rc = out_d(p->velz, S.vz))) return rc;
+    if (ctx->vel32) {
+        if ((rc = out_f(p->velx, S.vxf))) return rc;
+        if ((rc = out_f(p->vely, S.vyf))) return rc;
+        if ((rc = out_f(p->velz, S.vzf))) return rc;
+    } else {
+        if ((rc = out_d(p->velx, S.vx))) return rc;
+        if ((rc = out_d(p->vely, S.vy))) return rc;
+        if ((rc = out_d(p->velz, S.vz))) return rc;
+    }
     if ((rc = out_d(p->wx, S.wx))) return rc;
     if ((rc = out_d(p->wy, S.wy))) return rc;
     if ((rc = out_d(p->wz, S.wz))) return rc;
@@ -575,8 +604,9 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
 
 namespace {
 
-// Enqueue one DEM step reading buffer a.
-int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
+// Enqueue one DEM step reading buffer a.  resync: the FP32F sphere step
+// re-derives every slot's offsets and bin from its FP64 position.
+int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
 {
     const DevState &S = ctx->S;
     cudaStream_t st = ctx->stream;
@@ -604,7 +634,7 @@ int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a)
     if (!S.has_rods) {
         const Shape &sh = ctx->sh_sphere[precision == BMXG_FP32F ? 1 : 0];
         if (k0) cudaEventRecord(k0, st);
-        LAUNCH(launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st));
+        LAUNCH(launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st, resync));
         if (k1) cudaEventRecord(k1, st);
     } else {
         const int rg = grid_for(ctx, ctx->sh_rod, n);
@@ -626,11 +656,13 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
         *out = it->second;
         return BMXG_OK;
     }
+    // kResyncEvery steps (an even number, so the graph ends on the parity it
+    // starts from); the FP32F re-sync falls on its first step
     cudaGraph_t g = nullptr;
     const int64_t before = ctx->launches;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc1 = enqueue_step(ctx, dt, precision, parity);
-    int rc2 = rc1 ? rc1 : enqueue_step(ctx, dt, precision, parity ^ 1);
+    int rc2 = BMXG_OK;
+    for (int s = 0; s < kResyncEvery && !rc2; ++s) rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == 0);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc2) {
         if (g) cudaGraphDestroy(g);
@@ -667,23 +699,39 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int32_t left = nsteps;
     ctx->kev_used = 0;
-    if (left >= 2 && !ctx->profiling) {
-        cudaGraphExec_t g = nullptr;
-        int rc = get_graph(ctx, subdt, precision, ctx->parity, &g);
-        if (rc) return rc;
-        const int per = ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity}];
-        while (left >= 2) {
-            CK(cudaGraphLaunch(g, ctx->stream));
-            ctx->launches += per;
-            left -= 2;
-        }
-    }
-    while (left >= 1) {  // odd remainder, or every step in profiling mode
-        int rc = enqueue_step(ctx, subdt, precision, ctx->parity);
+    auto eager = [&]() -> int {  // one step outside a graph, on the re-sync schedule
+        int rc = enqueue_step(ctx, subdt, precision, ctx->parity, ctx->step_count % kResyncEvery == 0);
         if (rc) return rc;
         ctx->parity ^= 1;
+        ++ctx->step_count;
         --left;
+        return BMXG_OK;
+    };
+    // eager steps up to the next re-sync boundary, graph replays of
+    // kResyncEvery steps, eager remainder; every step eager when profiling
+    while (left > 0 && (ctx->profiling || ctx->step_count % kResyncEvery != 0 || left < kResyncEvery)) {
+        int rc = eager();
+        if (rc) return rc;
     }
+    if (left >= kResyncEvery) {
+        cudaGraphExec_t g = nullptr, g_other = nullptr;
+        int rc = get_graph(ctx, subdt, precision, ctx->parity, &g);
+        // the other parity's graph too, so that a later call needs no capture
+        if (!rc) rc = get_graph(ctx, subdt, precision, ctx->parity ^ 1, &g_other);
+        if (rc) return rc;
+        const int per = ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity}];
+        while (left >= kResyncEvery) {
+            CK(cudaGraphLaunch(g, ctx->stream));
+            ctx->launches += per;
+            ctx->step_count += kResyncEvery;
+            left -= kResyncEvery;
+        }
+    }
+    while (left > 0) {
+        int rc = eager();
+        if (rc) return rc;
+    }
+    ctx->vel32 = (precision == BMXG_FP32F) && !ctx->S.has_rods;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -844,10 +892,10 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
                 s.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
                 const int grd = grid_for(ctx, s, n);
                 for (int w = 0; w < 2; ++w)
-                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream));
+                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream, 0));
                 CK(cudaEventRecord(ctx->ev0, ctx->stream));
                 for (int r = 0; r < 5; ++r)
-                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream));
+                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream, 0));
                 CK(cudaEventRecord(ctx->ev1, ctx->stream));
                 CK(cudaEventSynchronize(ctx->ev1));
                 float ms = 0.0f;
@@ -1022,6 +1070,7 @@ int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
     ctx->traj_T = nsteps;
     ctx->traj_k = ckpt_every;
     ctx->traj_dt = subdt;
+    ctx->vel32 = false;
     ctx->stats.n_kernel_launches = ctx->launches;
     if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
     return BMXG_OK;

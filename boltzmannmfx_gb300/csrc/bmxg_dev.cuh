@@ -28,6 +28,8 @@ constexpr int BMXG_FP64_FORM = 0;               // BMXG_FP64 of bmxg.h
 constexpr int BMXG_FP32F_FORM = 1;              // BMXG_FP32F of bmxg.h
 constexpr int kYeast = 0, kFungi = 1;           // cellType (src/chemistry/bmx_chem.H:120-126)
 constexpr int kTip = 0, kSecond1 = 1, kSecond2 = 2, kInterior = 3;  // siteLocation (bmx_chem.H:128-136)
+constexpr int kWallTable = 66;                  // z-bins with a precomputed wall height (grown box)
+constexpr int kResyncEvery = 8;                 // FP32F: exact FP64 re-binning of every slot each 8th step
 
 // Geometry of one colony (an AMReX level geometry) plus its place in the
 // global column / slot numbering.
@@ -40,6 +42,13 @@ struct DevGeom {
     int slot_base;      // first slot of this colony
     int slot_end;       // one past the last slot
     int nbh_trivial;    // 1: BMXCheckPair's r^2 <= neighborhood holds for every stencil pair
+    float invny;        // 1 / n[1], for the column -> (x-bin, y-bin) split
+    int nwz;            // entries of wz (0: table not built, z too fine)
+    // height of each z-bin's lower face above the growth surface,
+    // (plo_z + (bz-1) dz) - z_wall, as an unevaluated float pair (hi + lo):
+    // the FP32 precision form evaluates the wall law from it and the particle's
+    // FP32 offset without FP64 arithmetic
+    float2 wz[kWallTable];
 };
 
 // Counters a step accumulates on the device.

@@ -31,6 +31,7 @@ struct DevState {
     int8_t *ctype;     // cell_type
 
     double *vx, *vy, *vz, *wx, *wy, *wz;  // step outputs (slot order)
+    float *vxf, *vyf, *vzf;               // velocity output of the FP32F sphere step
 
     // rod segments (null when the state holds spheres only)
     int has_rods;
@@ -67,6 +68,8 @@ int launch_gather_d(double *dst, const double *src, const int *perm, int n, int 
 int launch_gather_i(int *dst, const int *src, const int *perm, int n, int planes, int grid, int block, cudaStream_t st);
 int launch_gather_i8(int8_t *dst, const int *src, const int *perm, int n, int grid, int block, cudaStream_t st);
 int launch_scatter_d(double *dst, const double *src, const int *orig, int n, int grid, int block, cudaStream_t st);
+int launch_scatter_f2d(double *dst, const float *src, const int *orig, int n, int grid, int block,
+                       cudaStream_t st);
 int launch_scatter_i(int *dst, const int *src, const int *orig, int n, int planes, int grid, int block, cudaStream_t st);
 int launch_trig(const DevState &S, int b, int grid, int block, cudaStream_t st);
 
@@ -77,8 +80,10 @@ int launch_pairs(const DevState &S, const DevParams &P, int a, int64_t *cnt_or_o
 // ---- spheres (k_sphere.cu) -----------------------------------------------
 // force gather + wall + update + rebin of every slot, reading buffer a and
 // writing buffer b; precision BMXG_FP64 / BMXG_FP32F
+// resync (FP32F only): re-derive every slot's FP32 offsets and bin from its
+// FP64 position this step
 int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision,
-                        int grid, int block, cudaStream_t st);
+                        int grid, int block, cudaStream_t st, int resync = 1);
 
 // ---- rods and mixed states (k_rod.cu) ------------------------------------
 int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st);

@@ -45,7 +45,8 @@ __device__ __forceinline__ void visit_stencil(const DevState &S, const DevGeom &
             for (int t = __ldg(&cs[cc]); t < t1; ++t) {
                 const int j = __ldg(&perm[t]);
                 const int dzs = __ldg(&izs[j]) - izi;
-                if (dzs < -1 || dzs > 1) continue;
+                if (dzs > 1) break;  // a column is sorted by z-bin: the rest is out of reach
+                if (dzs < -1) continue;
                 if (j == i) continue;
                 if ((sx | sy) && !image_in_row(S, G, a, j, ii, jj, sx, sy)) continue;
                 f(j, ii - bx, jj - by, dzs, sx, sy);

@@ -198,6 +198,12 @@ __global__ void k_scatter_d(double *dst, const double *src, const int *orig, int
         dst[orig[s]] = src[s];
 }
 
+__global__ void k_scatter_f2d(double *dst, const float *src, const int *orig, int n)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        dst[orig[s]] = (double)src[s];
+}
+
 __global__ void k_scatter_i(int *dst, const int *src, const int *orig, int n, int planes)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -324,6 +330,13 @@ int launch_scatter_d(double *dst, const double *src, const int *orig, int n, int
                       cudaStream_t st)
 {
     k_scatter_d<<<grid, block, 0, st>>>(dst, src, orig, n);
+    return 1;
+}
+
+int launch_scatter_f2d(double *dst, const float *src, const int *orig, int n, int grid, int block,
+                       cudaStream_t st)
+{
+    k_scatter_f2d<<<grid, block, 0, st>>>(dst, src, orig, n);
     return 1;
 }
 

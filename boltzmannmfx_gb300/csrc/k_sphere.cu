@@ -8,17 +8,22 @@
 // the periodic wrap of the trailing Redistribute (:485-486).
 //
 // Forms:
-//  FP64  (plain)  every pair that can pass the reference's cutoff test is
-//                 evaluated in FP64 with the reference's operation order
-//                 (this file is compiled with -fmad=false), accumulated in
-//                 list order: the result is bit-identical to the host
-//                 oracle.  Pairs are first screened in FP32 from the
-//                 bin-relative offsets with an absolute slack that bounds the
-//                 FP32 error, so only pairs that are certainly beyond the
-//                 cutoff skip the FP64 test.
-//  FP32F (precision form) pair math in FP32 on FP64-differenced bin-relative
-//                 offsets; the wall force and the position accumulation stay
-//                 FP64.
+//  FP64  (plain, k_sphere64) every pair that can pass the reference's cutoff
+//        test is evaluated in FP64 with the reference's operation order (this
+//        file is compiled with -fmad=false), accumulated in list order: the
+//        result is bit-identical to the host oracle.  Pairs are first
+//        screened in FP32 from the bin-relative offsets with an absolute
+//        slack that bounds the FP32 error, so only pairs that are certainly
+//        beyond the cutoff skip the FP64 test.
+//  FP32F (precision form, k_sphere32) pair math and wall law in FP32 on
+//        FP64-differenced bin-relative offsets; the position accumulation
+//        stays FP64.  GB300 issues FP64 at 1/64 of the FP32 rate, so the
+//        per-particle epilogue avoids FP64 too: the bin-relative offsets are
+//        advanced in FP32 and re-derived exactly from the FP64 position
+//        (exact FP64 re-binning) every kResyncEvery-th step and whenever a
+//        particle comes within a guard band of a bin face, where its bin
+//        might change.  Away from the faces the FP64 bin cannot change, so
+//        the neighbour lists stay exactly the reference's.
 // Roofline: HBM / L2 bound gather; no dense contraction, so no tensor cores.
 #include "bmxg_stencil.cuh"
 
@@ -26,12 +31,9 @@ namespace bmxg {
 
 namespace {
 
-template <int PREC>
-__global__ void __launch_bounds__(256) k_sphere(const DevState S, const DevParams P, double dt, int a)
+__global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)
 {
     const int b = a ^ 1;
-    const float bwf = (float)P.bw;
-    const float kf = (float)P.k;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, i);
         int bx, by;
@@ -44,57 +46,31 @@ __global__ void __launch_bounds__(256) k_sphere(const DevState S, const DevParam
         // absolute slack bounding the FP32 distance error (offsets + bin widths)
         const float slack = 8.0f * 1.1920929e-7f * fmaxf(dxb, fmaxf(dyb, dzb));
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
         visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
             const float4 q = __ldg(&S.rel[a][j]);
             const float ex = (me.x - q.x) - (float)dxs * dxb;
             const float ey = (me.y - q.y) - (float)dys * dyb;
             const float ez = (me.z - q.z) - (float)dzs * dzb;
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float rAf = __fadd_rn(__fadd_rn(me.w, q.w), bwf);
-            if (PREC == BMXG_FP64_FORM) {
-                const float lim = __fadd_rn(rAf, slack);
-                if (r2f > __fmul_rn(lim, lim)) return;
-                const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
-                const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
-                const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;  // not in the neighbour list
-                const double rj = S.rad[j];
-                const double rlm = ri + rj + P.bw;                // maxInteractionDistance
-                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
-                const double rS = ri + rj;
-                const double rA = rS + P.bw;
-                const double rn = sqrt(r2);
-                const double ux = dx / rn, uy = dy / rn, uz = dz / rn;
-                const double F = (rn < rA) ? -P.k * (rn - rA) * (rn - rA) * (rn - rS) : 0.0;
-                fx += F * ux;
-                fy += F * uy;
-                fz += F * uz;
-            } else {
-                if (!(r2f < __fmul_rn(rAf, rAf))) return;
-                if (!G.nbh_trivial) {
-                    const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
-                    const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
-                    const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
-                    if (!(dx * dx + dy * dy + dz * dz <= P.nbh)) return;
-                }
-                const float inv = rsqrtf(r2f);
-                const float rn = __fmul_rn(r2f, inv);
-                const float rSf = __fadd_rn(me.w, q.w);
-                const float d1 = __fsub_rn(rn, rAf);
-                const float F = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
-                const float Fi = __fmul_rn(F, inv);
-                gx = __fmaf_rn(Fi, ex, gx);
-                gy = __fmaf_rn(Fi, ey, gy);
-                gz = __fmaf_rn(Fi, ez, gz);
-            }
+            const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), (float)P.bw), slack);
+            if (r2f > __fmul_rn(lim, lim)) return;
+            const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
+            const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
+            const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (!G.nbh_trivial && !(r2 <= P.nbh)) return;  // not in the neighbour list
+            const double rj = S.rad[j];
+            const double rlm = ri + rj + P.bw;                // maxInteractionDistance
+            if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+            const double rS = ri + rj;
+            const double rA = rS + P.bw;
+            const double rn = sqrt(r2);
+            const double ux = dx / rn, uy = dy / rn, uz = dz / rn;
+            const double F = (rn < rA) ? -P.k * (rn - rA) * (rn - rA) * (rn - rS) : 0.0;
+            fx += F * ux;
+            fy += F * uy;
+            fz += F * uz;
         });
-        if (PREC != BMXG_FP64_FORM) {
-            fx = (double)gx;
-            fy = (double)gy;
-            fz = (double)gz;
-        }
         // evaluateSurfaceForce, sphere branch: vcom = (0, 0, wall), vrot = 0
         const double vx = fx + 0.0;
         const double vy = fy + 0.0;
@@ -114,15 +90,121 @@ __global__ void __launch_bounds__(256) k_sphere(const DevState S, const DevParam
     }
 }
 
+// Exact float -> double conversion with integer operations (GB300's FP64
+// pipe is the scarce resource here).  Subnormal floats flush to zero.
+__device__ __forceinline__ double f2d_int(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0u) return __longlong_as_double((long long)s);
+    const unsigned long long ee = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);  // 1023 - 127
+    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+    return __longlong_as_double((long long)(s | (ee << 52) | m));
+}
+
+// growth-surface cubic law in FP32 (bmx_cell_interaction_K.H:1019-1030)
+__device__ __forceinline__ float wall_law32(float dz, float rS, float zk, float zbw, float zg)
+{
+    const float rA = rS + zbw;
+    float v;
+    if (dz > 0.0f && dz < rA) v = -zk * (dz - rA) * (dz - rA) * (dz - rS);
+    else if (dz <= 0.0f) v = zk * rA * rA * rS;
+    else v = 0.0f;
+    return v - zg * zk * rA * rA * rS;
+}
+
+__global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, double dt, int a,
+                                                  int resync)
+{
+    const int b = a ^ 1;
+    const float bwf = (float)P.bw, kf = (float)P.k, dtf = (float)dt;
+    const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        const int col = S.col[a][i];
+        int bx, by;
+        col_to_bxy(G, col, bx, by);
+        const int izi = S.iz[a][i];
+        const float4 me = S.rel[a][i];
+        const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
+        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+        visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
+            const float4 q = __ldg(&S.rel[a][j]);
+            const float ex = (me.x - q.x) - (float)dxs * dxb;
+            const float ey = (me.y - q.y) - (float)dys * dyb;
+            const float ez = (me.z - q.z) - (float)dzs * dzb;
+            const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+            const float rAf = __fadd_rn(__fadd_rn(me.w, q.w), bwf);
+            if (!(r2f < __fmul_rn(rAf, rAf))) return;
+            if (!G.nbh_trivial) {  // BMXCheckPair, exactly (FP64)
+                const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
+                const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
+                const double dx = S.x[a][i] - xj, dy = S.y[a][i] - yj, dz = S.z[a][i] - S.z[a][j];
+                if (!(dx * dx + dy * dy + dz * dz <= P.nbh)) return;
+            }
+            const float inv = rsqrtf(r2f);
+            const float rn = __fmul_rn(r2f, inv);
+            const float rSf = __fadd_rn(me.w, q.w);
+            const float d1 = __fsub_rn(rn, rAf);
+            const float F = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
+            const float Fi = __fmul_rn(F, inv);
+            gx = __fmaf_rn(Fi, ex, gx);
+            gy = __fmaf_rn(Fi, ey, gy);
+            gz = __fmaf_rn(Fi, ez, gz);
+        });
+        // wall: height above the surface from the bin face's height (float
+        // pair) and the FP32 offset, FP64 only where no table entry exists
+        float dzw;
+        if (izi < G.nwz) {
+            const float2 c = G.wz[izi];
+            dzw = (c.x + me.z) + c.y;
+        } else {
+            dzw = (float)(S.z[a][i] - P.z_wall);
+        }
+        const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, me.w, zkf, zbwf, zgf);
+        const float ix = dtf * vx, iy = dtf * vy, iz = dtf * vz;
+        // FP64 position accumulation
+        double nx = S.x[a][i] + f2d_int(ix);
+        double ny = S.y[a][i] + f2d_int(iy);
+        const double nz = S.z[a][i] + f2d_int(iz);
+        S.vxf[i] = vx;
+        S.vyf[i] = vy;
+        S.vzf[i] = vz;
+        // FP32 offsets; exact FP64 re-binning near a bin face or on re-sync steps
+        const float4 r = make_float4(me.x + ix, me.y + iy, me.z + iz, me.w);
+        const float g0 = 1e-4f * dxb, g1 = 1e-4f * dyb, g2 = 1e-4f * dzb;
+        const bool inside = !resync && r.x >= g0 && r.x <= dxb - g0 && r.y >= g1 && r.y <= dyb - g1 &&
+                            r.z >= g2 && r.z <= dzb - g2;
+        if (inside) {
+            S.x[b][i] = nx;
+            S.y[b][i] = ny;
+            S.z[b][i] = nz;
+            S.rel[b][i] = r;
+            S.col[b][i] = col;
+            S.iz[b][i] = izi;
+            atomicAdd(&S.colcnt[col], 1);
+            if (!isfinite(vx + vy + vz)) atomicAdd(&S.cnt->nonfinite, 1ULL);
+        } else {
+            if (G.per[0]) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
+            if (G.per[1]) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+            S.x[b][i] = nx;
+            S.y[b][i] = ny;
+            S.z[b][i] = nz;
+            rebin_slot(S, G, i, nx, ny, nz, S.rad[i], b);
+        }
+    }
+}
+
 }  // namespace
 
 int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision, int grid,
-                        int block, cudaStream_t st)
+                       int block, cudaStream_t st, int resync)
 {
     if (precision == BMXG_FP64_FORM)
-        k_sphere<BMXG_FP64_FORM><<<grid, block, 0, st>>>(S, P, dt, a);
+        k_sphere64<<<grid, block, 0, st>>>(S, P, dt, a);
     else
-        k_sphere<BMXG_FP32F_FORM><<<grid, block, 0, st>>>(S, P, dt, a);
+        k_sphere32<<<grid, block, 0, st>>>(S, P, dt, a, resync);
     return 1;
 }
 

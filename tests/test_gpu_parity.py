@@ -172,3 +172,29 @@ def test_evolve_particles_dropin(gpu_lib):
     ctx = gpu_ctx(w.params, w.geoms, w.particles)
     cost, nsub = ctx.evolve_particles(w.dt)
     assert nsub == 1 and cost == [float(w.n)]
+
+
+def test_fp32f_multistep_bins_stay_exact(gpu_lib, oracle_lib):
+    """50 FP32F steps (several FP32-offset re-sync periods): the neighbour list
+    of the resulting FP64 positions is still exactly the reference's, and the
+    displacements follow the FP64 trajectory."""
+    w = configs.sphere_fp32(n=40_000)
+    g = w.geoms[0]
+    ctx32 = gpu_ctx(w.params, [g], w.particles)
+    ctx64 = gpu_ctx(w.params, [g], w.particles)
+    ctx32.step(w.dt, 50, BMXG_FP32F)
+    ctx64.step(w.dt, 50, BMXG_FP64)
+    A = readback(ctx32, w.particles)
+    B = readback(ctx64, w.particles)
+    assert same_pairs(ctx32.pairs(), oracle_lib.pairs(w.params, g, A))
+    L = g.prob_hi[0] - g.prob_lo[0]
+    for k in ("x", "y", "z"):
+        da = A[k] - w.particles[k]
+        db = B[k] - w.particles[k]
+        if k != "z":  # periodic wrap: compare displacements modulo the box
+            da = (da + L / 2) % L - L / 2
+            db = (db + L / 2) % L - L / 2
+        assert relerr(da, db) <= 1e-4, k
+    v32 = np.stack([A["velx"], A["vely"], A["velz"]])
+    v64 = np.stack([B["velx"], B["vely"], B["velz"]])
+    assert relerr(v32, v64) <= 1e-4
