@@ -407,6 +407,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         AL(S.x[k], n); AL(S.y[k], n); AL(S.z[k], n);
         AL(S.rel[k], n); AL(S.col[k], n); AL(S.iz[k], n);
         AL(S.perm[k], n); AL(S.colstart[k], ncols + 1);
+        AL(S.srel[k], n); AL(S.siz[k], n); AL(S.rank[k], n);
     }
     AL(S.colcnt, ncols); AL(S.tmp, n);
     AL(S.rad, n); AL(S.orig, n); AL(S.ctype, n);
@@ -836,6 +837,37 @@ int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int6
     cudaError_t e2 = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, cudaGetErrorString(e));
+    return BMXG_OK;
+}
+
+int bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
+    if (added) *added = 0;
+    if (overflow) *overflow = 0;
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (!(rlim > 0.0)) rlim = 1.0e-7;
+    if (ctx->n == 0 || !ctx->S.has_rods) return BMXG_OK;
+    cudaStream_t st = ctx->stream;
+    const DevParams P = dev_params(ctx->prm);
+    unsigned long long *d_cnt = nullptr;
+    CK(cudaMallocAsync((void **)&d_cnt, 2 * sizeof(unsigned long long), st));
+    unsigned long long h_cnt[2] = {0, 0};
+    cudaError_t e = cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) {
+        const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, ctx->n);
+        ctx->launches += launch_init_bonds(ctx->S, P, ctx->parity, rlim, d_cnt, grd, blk, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_cnt, d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d_cnt, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, cudaGetErrorString(e));
+    if (added) *added = (int64_t)h_cnt[0];
+    if (overflow) *overflow = (int64_t)h_cnt[1];
+    if (h_cnt[1]) return fail(ctx, BMXG_ERR_CAPACITY, "a segment end met more bonds than its four table slots");
     return BMXG_OK;
 }
 

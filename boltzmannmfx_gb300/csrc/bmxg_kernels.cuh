@@ -25,6 +25,12 @@ struct DevState {
     int *colstart[2];  // ncols_total + 1 offsets into perm
     int *colcnt;       // per-column counter, zero between uses
     int *tmp;          // scatter scratch, n entries
+    // column-sorted copies (optional: null skips them): srel[t] = rel[perm[t]],
+    // siz[t] = iz[perm[t]], rank[perm[t]] = t; the sphere kernels walk these
+    // contiguously instead of chasing perm
+    float4 *srel[2];
+    int *siz[2];
+    int *rank[2];
 
     double *rad;
     int *orig;         // slot -> caller's index
@@ -90,6 +96,9 @@ int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int 
 int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
                       cudaStream_t st);
 int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st);
+// start-up bond detection; counts[0] += bonds added, counts[1] += bonds past four
+int launch_init_bonds(const DevState &S, const DevParams &P, int a, double rlim, unsigned long long *counts,
+                      int grid, int block, cudaStream_t st);
 
 // ---- differentiation form (k_adjoint.cu) ---------------------------------
 int launch_dfwd(const DevState &S, const DevParams &P, const DiffParams &D, double dt, int a, int grid, int block,

@@ -55,6 +55,60 @@ __device__ __forceinline__ void visit_stencil(const DevState &S, const DevGeom &
     }
 }
 
+// The same walk over the column-sorted copies (siz / srel, filled by the
+// rebuild): f(t, dxs, dys, dzs, sx, sy) gets the sorted index t of each
+// candidate (its slot is perm[t]).  An x-row's three columns by-1..by+1 are
+// consecutive column ids, so away from the periodic faces a row is three
+// back-to-back runs of one contiguous range; each run is ordered by z-bin
+// and stops at the first entry above izi + 1.  self_t = rank of the slot
+// itself.  Order of candidates: identical to visit_stencil.
+template <class F>
+__device__ __forceinline__ void visit_sorted(const DevState &S, const DevGeom &G, int a, int self_t, int bx,
+                                             int by, int izi, F &&f)
+{
+    const int *__restrict__ cs = S.colstart[a];
+    const int *__restrict__ siz = S.siz[a];
+    for (int ii = bx - 1; ii <= bx + 1; ++ii) {
+        int srcx = ii, sx = 0;
+        if (ii == 0) {
+            if (!G.per[0]) continue;
+            srcx = G.n[0];
+            sx = -1;
+        } else if (ii == G.n[0] + 1) {
+            if (!G.per[0]) continue;
+            srcx = 1;
+            sx = 1;
+        }
+        if (sx == 0 && by >= 2 && by <= G.n[1] - 1) {
+            const int c = column_of(G, srcx, by - 1);
+            int lo = __ldg(&cs[c]);
+            for (int dys = -1; dys <= 1; ++dys) {
+                const int hi = __ldg(&cs[c + dys + 2]);
+                for (int t = lo; t < hi; ++t) {
+                    const int dzs = __ldg(&siz[t]) - izi;
+                    if (dzs > 1) break;
+                    if (dzs < -1 || t == self_t) continue;
+                    f(t, ii - bx, dys, dzs, 0, 0);
+                }
+                lo = hi;
+            }
+        } else {
+            for (int jj = by - 1; jj <= by + 1; ++jj) {
+                int cc, ssx, sy;
+                if (!stencil_row(G, ii, jj, cc, ssx, sy)) continue;
+                const int t1 = __ldg(&cs[cc + 1]);
+                for (int t = __ldg(&cs[cc]); t < t1; ++t) {
+                    const int dzs = __ldg(&siz[t]) - izi;
+                    if (dzs > 1) break;
+                    if (dzs < -1 || t == self_t) continue;
+                    if ((ssx | sy) && !image_in_row(S, G, a, __ldg(&S.perm[a][t]), ii, jj, ssx, sy)) continue;
+                    f(t, ii - bx, jj - by, dzs, ssx, sy);
+                }
+            }
+        }
+    }
+}
+
 // Grown-box bin (bx, by) of a slot from its column id.
 __device__ __forceinline__ void col_to_bxy(const DevGeom &G, int col, int &bx, int &by)
 {

@@ -121,13 +121,20 @@ __global__ void k_canon(const DevState S, int b)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const int c = S.col[b][i];
         const int s0 = S.colstart[b][c], s1 = S.colstart[b][c + 1];
-        const unsigned long long key = col_key(S.iz[b][i], S.orig[i]);
+        const int izi = S.iz[b][i];
+        const unsigned long long key = col_key(izi, S.orig[i]);
         int rank = 0;
         for (int t = s0; t < s1; ++t) {
             const int j = S.tmp[t];
             rank += (col_key(S.iz[b][j], S.orig[j]) < key);
         }
-        S.perm[b][s0 + rank] = i;
+        const int t = s0 + rank;
+        S.perm[b][t] = i;
+        if (S.srel[b]) {
+            S.srel[b][t] = S.rel[b][i];
+            S.siz[b][t] = izi;
+            S.rank[b][i] = t;
+        }
     }
 }
 

@@ -496,6 +496,71 @@ __global__ void k_rod_update(const DevState S, double dt, int a)
     }
 }
 
+// ---- InitBonds ---------------------------------------------------------------
+// Start-up bond detection (bmx_pc_interaction.cpp:500-626 with fixBonds,
+// bmx_cell_interaction_K.H:1287-1440): for every listed FUNGI-FUNGI pair
+// within the interaction gate, the four end pairs (i1,j1), (i2,j1), (i1,j2),
+// (i2,j2) are tried in that order and the first closer than rlim appends
+// (id_j, cpu_j, site of i) to i's table.  As in the force gather, the
+// neighbour is a copy, so only i's own table changes; each thread owns its
+// row and appends in the reference's list order.  A fifth bond (past the
+// reference's four table slots) is counted, not written.
+__global__ void k_init_bonds(const DevState S, const DevParams P, int a, double rlim,
+                             unsigned long long *counts)
+{
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (S.ctype[i] != kFungi) continue;
+        const DevGeom &G = geom_of(S, i);
+        int bx, by;
+        col_to_bxy(G, S.col[a][i], bx, by);
+        const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
+        const double Li = S.clen[i];
+        const double4 tri = S.trig[a][i];
+        const double ni[3] = {tri.y * tri.z, tri.y * tri.w, tri.x};
+        int nb = S.tab[a][i];
+        unsigned long long add = 0, over = 0;
+        visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+            if (S.ctype[j] != kFungi) return;
+            double d[3];
+            const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+            if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
+            const double Lj = S.clen[j];
+            const double rlm = 1.5 * (Li + Lj) + P.bw;
+            if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+            const double4 trj = S.trig[a][j];
+            const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
+            double e[4][3];  // i1, i2, j1, j2 with j's centre at the origin
+            for (int k = 0; k < 3; ++k) {
+                e[0][k] = d[k] - 0.5 * ni[k] * Li;
+                e[1][k] = d[k] + 0.5 * ni[k] * Li;
+                e[2][k] = -0.5 * nj[k] * Lj;
+                e[3][k] = 0.5 * nj[k] * Lj;
+            }
+            for (int m = 0; m < 4; ++m) {
+                const int si = (m & 1) + 1, sj = (m >> 1) + 1;  // (1,1) (2,1) (1,2) (2,2)
+                const double *p = e[si - 1], *q = e[1 + sj];
+                const double rx = p[0] - q[0], ry = p[1] - q[1], rz = p[2] - q[2];
+                if (sqrt(rx * rx + ry * ry + rz * rz) < rlim) {
+                    if (nb >= 0 && nb < 4) {
+                        S.tab[a][(size_t)(1 + nb) * n + i] = S.id[j];
+                        S.tab[a][(size_t)(5 + nb) * n + i] = S.cpu[j];
+                        S.tab[a][(size_t)(9 + nb) * n + i] = si;
+                        ++nb;
+                        ++add;
+                    } else {
+                        ++over;
+                    }
+                    break;
+                }
+            }
+        });
+        S.tab[a][i] = nb;
+        if (add) atomicAdd(&counts[0], add);
+        if (over) atomicAdd(&counts[1], over);
+    }
+}
+
 }  // namespace
 
 int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st)
@@ -517,6 +582,13 @@ int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision
 int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st)
 {
     k_rod_update<<<grid, block, 0, st>>>(S, dt, a);
+    return 1;
+}
+
+int launch_init_bonds(const DevState &S, const DevParams &P, int a, double rlim, unsigned long long *counts,
+                      int grid, int block, cudaStream_t st)
+{
+    k_init_bonds<<<grid, block, 0, st>>>(S, P, a, rlim, counts);
     return 1;
 }
 

@@ -31,6 +31,25 @@ namespace bmxg {
 
 namespace {
 
+// Walk the stencil over the column-sorted copies when the state has them
+// (SORTED), else over perm (callers that provide no sorted buffers).  f gets
+// the candidate's FP32 offsets, a functor returning its slot, and the shifts.
+template <bool SORTED, class F>
+__device__ __forceinline__ void walk(const DevState &S, const DevGeom &G, int a, int i, int bx, int by, int izi,
+                                     F &&f)
+{
+    if constexpr (SORTED) {
+        visit_sorted(S, G, a, S.rank[a][i], bx, by, izi, [&](int t, int dxs, int dys, int dzs, int sx, int sy) {
+            f(__ldg(&S.srel[a][t]), [&]() { return __ldg(&S.perm[a][t]); }, dxs, dys, dzs, sx, sy);
+        });
+    } else {
+        visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
+            f(__ldg(&S.rel[a][j]), [&]() { return j; }, dxs, dys, dzs, sx, sy);
+        });
+    }
+}
+
+template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)
 {
     const int b = a ^ 1;
@@ -46,14 +65,14 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
         // absolute slack bounding the FP32 distance error (offsets + bin widths)
         const float slack = 8.0f * 1.1920929e-7f * fmaxf(dxb, fmaxf(dyb, dzb));
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
-            const float4 q = __ldg(&S.rel[a][j]);
+        walk<SORTED>(S, G, a, i, bx, by, izi, [&](const float4 q, auto slot, int dxs, int dys, int dzs, int sx, int sy) {
             const float ex = (me.x - q.x) - (float)dxs * dxb;
             const float ey = (me.y - q.y) - (float)dys * dyb;
             const float ez = (me.z - q.z) - (float)dzs * dzb;
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
             const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), (float)P.bw), slack);
             if (r2f > __fmul_rn(lim, lim)) return;
+            const int j = slot();
             const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
             const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
             const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
@@ -114,6 +133,7 @@ __device__ __forceinline__ float wall_law32(float dz, float rS, float zk, float 
     return v - zg * zk * rA * rA * rS;
 }
 
+template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, double dt, int a,
                                                   int resync)
 {
@@ -129,8 +149,7 @@ __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevPar
         const float4 me = S.rel[a][i];
         const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
         float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-        visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
-            const float4 q = __ldg(&S.rel[a][j]);
+        walk<SORTED>(S, G, a, i, bx, by, izi, [&](const float4 q, auto slot, int dxs, int dys, int dzs, int sx, int sy) {
             const float ex = (me.x - q.x) - (float)dxs * dxb;
             const float ey = (me.y - q.y) - (float)dys * dyb;
             const float ez = (me.z - q.z) - (float)dzs * dzb;
@@ -138,6 +157,7 @@ __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevPar
             const float rAf = __fadd_rn(__fadd_rn(me.w, q.w), bwf);
             if (!(r2f < __fmul_rn(rAf, rAf))) return;
             if (!G.nbh_trivial) {  // BMXCheckPair, exactly (FP64)
+                const int j = slot();
                 const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
                 const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
                 const double dx = S.x[a][i] - xj, dy = S.y[a][i] - yj, dz = S.z[a][i] - S.z[a][j];
@@ -201,10 +221,14 @@ __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevPar
 int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision, int grid,
                        int block, cudaStream_t st, int resync)
 {
-    if (precision == BMXG_FP64_FORM)
-        k_sphere64<<<grid, block, 0, st>>>(S, P, dt, a);
-    else
-        k_sphere32<<<grid, block, 0, st>>>(S, P, dt, a, resync);
+    const bool sorted = S.srel[a] != nullptr;  // the context keeps sorted copies; bare callers do not
+    if (precision == BMXG_FP64_FORM) {
+        if (sorted) k_sphere64<true><<<grid, block, 0, st>>>(S, P, dt, a);
+        else k_sphere64<false><<<grid, block, 0, st>>>(S, P, dt, a);
+    } else {
+        if (sorted) k_sphere32<true><<<grid, block, 0, st>>>(S, P, dt, a, resync);
+        else k_sphere32<false><<<grid, block, 0, st>>>(S, P, dt, a, resync);
+    }
     return 1;
 }
 

@@ -24,7 +24,7 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
                "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
-               "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_autotune")
+               "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_autotune")
 
 
 class Ext(C.Structure):
@@ -68,6 +68,7 @@ def load_library(path=None):
     L.bmxg_get_pairs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int8),
                                  C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
+    L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
     L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
         [C.c_double, vp]
@@ -171,6 +172,17 @@ class Context:
                                             idx.ctypes.data_as(C.POINTER(C.c_int32)),
                                             img.ctypes.data_as(C.POINTER(C.c_int8)), cap, C.byref(total)))
         return offs, idx[:total.value], img[:total.value]
+
+    def init_bonds(self, rlim=1.0e-7):
+        """InitBonds on the loaded state (bond tables of coincident segment
+        ends).  Returns (added, overflow); raises BmxgError when a table is full."""
+        added = C.c_int64(0)
+        over = C.c_int64(0)
+        rc = self.lib.bmxg_init_bonds(self.h, rlim, C.byref(added), C.byref(over))
+        if rc == abi.BMXG_ERR_CAPACITY:
+            raise BmxgError(rc, f"InitBonds: {over.value} bonds found a full table ({added.value} added)")
+        self._check(rc)
+        return added.value, over.value
 
     def set_ext(self, damping=0.0, mu=0.0, adhesion=None):
         e = Ext()

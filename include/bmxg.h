@@ -283,6 +283,22 @@ int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *ge
                               double *vel_x, double *vel_y, double *vel_z,
                               double dt, void *stream);
 
+/* ---- start-up bonds ----------------------------------------------------- */
+
+/* InitBonds on the CURRENT state: for every FUNGI-FUNGI pair of the step's
+ * neighbour list within the interaction gate, the first of the end pairs
+ * (site1,site1), (site2,site1), (site1,site2), (site2,site2) closer than rlim
+ * appends (id, cpu of the neighbour, site of the segment) to the segment's
+ * own bond table.  rlim <= 0 selects the reference's 1e-7.  Replaces
+ * BMXParticleContainer::InitBonds (src/des/bmx_pc_interaction.cpp:500-668,
+ * with fixBonds of src/chemistry/bmx_cell_interaction_K.H:1287-1440), which
+ * src/timestepping/bmx_evolve.cpp:95 calls once at time 0.  The neighbour's
+ * side is written to a copy in the reference and discarded, as here.
+ * *added / *overflow (may be NULL) receive the bonds appended and those that
+ * found the table full; the reference writes the latter past its four slots,
+ * here they are dropped and the call returns BMXG_ERR_CAPACITY. */
+int  bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* Time the launch shapes of the step kernels on the loaded state and keep

@@ -840,3 +840,76 @@ double orc_time_evolve(const bmxg_params *prm, int32_t ncol,
     if (rc) return -1.0;
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+/* ------------------------------------------------------------------------ */
+/* InitBonds (src/des/bmx_pc_interaction.cpp:500-668) with fixBonds          */
+/* (src/chemistry/bmx_cell_interaction_K.H:1285-1444), restated              */
+/* ------------------------------------------------------------------------ */
+
+/* For every FUNGI segment i, in list order over its gated FUNGI neighbours
+ * j, the first pair of ends (i1-j1, i2-j1, i1-j2, i2-j2) closer than rlim
+ * appends (id_j, cpu_j, site of i) to i's bond table.  fixBonds also writes
+ * j's table, but j is the loop's by-value copy (bmx_pc_interaction.cpp:591),
+ * so only i's table changes.  fixBonds does not check the table's capacity
+ * (it would write past seg4); here a fifth bond is not stored and counted
+ * in *overflow instead. */
+int orc_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_particles *p,
+                   const int64_t *offs, const int32_t *idx, const int8_t *img, double rlim,
+                   int64_t *added, int64_t *overflow)
+{
+    og_t g;
+    int rc = og_init(geom, &g);
+    if (rc) return rc;
+    if (!prm || !p || !offs || p->n < 0) return BMXG_ERR_ARG;
+    if (!has_rod_fields(p)) return BMXG_ERR_ARG;
+    const int64_t N = p->n;
+    int64_t nadd = 0, nover = 0;
+    for (int64_t i = 0; i < N; ++i) {
+        if (p->cell_type[i] != BMXG_FUNGI) continue;
+        for (int64_t t = offs[i]; t < offs[i + 1]; ++t) {
+            int64_t j = idx[t];
+            if (p->cell_type[j] != BMXG_FUNGI) continue;
+            int sx = img[t] % 3 - 1, sy = img[t] / 3 - 1;
+            double r12[3];
+            r12[0] = p->x[i] - (sx ? p->x[j] + (double)sx * g.len[0] : p->x[j]);
+            r12[1] = p->y[i] - (sy ? p->y[j] + (double)sy * g.len[1] : p->y[j]);
+            r12[2] = p->z[i] - p->z[j];
+            double r2 = r12[0] * r12[0] + r12[1] * r12[1] + r12[2] * r12[2];
+            double rlm = max_dist(p, i, j, prm->bndry_width);
+            if (!(r2 <= (rlm - 1.0e-15) * (rlm - 1.0e-15))) continue;
+            double Ri[3][3], Rj[3][3], ni[3], nj[3];
+            frame(p->theta[i], p->phi[i], Ri, ni);
+            frame(p->theta[j], p->phi[j], Rj, nj);
+            double e[4][3];  /* i1, i2, j1, j2 (j at the origin) */
+            for (int k = 0; k < 3; ++k) {
+                e[0][k] = r12[k] - 0.5 * ni[k] * p->c_length[i];
+                e[1][k] = r12[k] + 0.5 * ni[k] * p->c_length[i];
+                e[2][k] = -0.5 * nj[k] * p->c_length[j];
+                e[3][k] = 0.5 * nj[k] * p->c_length[j];
+            }
+            /* (site of i, site of j) in the order fixBonds tries them */
+            static const int order[4][2] = {{1, 1}, {2, 1}, {1, 2}, {2, 2}};
+            for (int m = 0; m < 4; ++m) {
+                const double *a = e[order[m][0] - 1], *b = e[1 + order[m][1]];
+                double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+                double r = sqrt(dx * dx + dy * dy + dz * dz);
+                if (r < rlim) {
+                    int nb = p->n_bnds[i];
+                    if (nb >= 0 && nb < 4) {
+                        p->seg_id1[nb * N + i] = p->id[j];
+                        p->seg_id2[nb * N + i] = p->cpu[j];
+                        p->site[nb * N + i] = order[m][0];
+                        p->n_bnds[i] = nb + 1;
+                        ++nadd;
+                    } else {
+                        ++nover;
+                    }
+                    break;
+                }
+            }
+        }
+    }
+    if (added) *added = nadd;
+    if (overflow) *overflow = nover;
+    return BMXG_OK;
+}

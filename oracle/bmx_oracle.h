@@ -60,6 +60,12 @@ double orc_time_evolve(const bmxg_params *prm, int32_t ncol,
                        bmxg_particles *p, double dt, int32_t nsteps,
                        int nthreads);
 
+/* InitBonds: bond segments whose ends are closer than rlim (1e-7 in the
+ * reference, bmx_pc_interaction.cpp:508), over the given neighbour list. */
+int  orc_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_particles *p,
+                    const int64_t *offs, const int32_t *idx, const int8_t *img, double rlim,
+                    int64_t *added, int64_t *overflow);
+
 /* Single-pair / single-particle entry points used by unit tests. */
 void orc_pair_force(const bmxg_params *prm, const double r12[3],
                     const bmxg_particles *p, int64_t i, int64_t j,

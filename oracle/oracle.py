@@ -61,6 +61,7 @@ def lib():
         L.orc_surface_force.restype = None
         L.orc_min_distance.argtypes = [_d, _d, _d]
         L.orc_min_distance.restype = None
+        L.orc_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double, _i64, _i64]
         _lib = L
     return _lib
 
@@ -86,6 +87,7 @@ def reflib():
         L.ref_pair_force.restype = None
         L.ref_surface_force.argtypes = [_P, _S, C.c_int64, _d, _d]
         L.ref_surface_force.restype = None
+        L.ref_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double]
         _ref = L
     return _ref
 
@@ -205,3 +207,42 @@ def surface_force(params, P, i, use_ref=False):
     f = reflib().ref_surface_force if use_ref else lib().orc_surface_force
     f(C.byref(params), C.byref(P.struct()), i, _dp(v), _dp(w))
     return v, w
+
+
+RLIM = 1.0e-7  # InitBonds' bond-detection distance (src/des/bmx_pc_interaction.cpp:508)
+
+
+def init_bonds(params, geom, P, pl=None, rlim=RLIM, use_ref=False):
+    """Bond segments whose ends are closer than rlim; mutates P's bond tables.
+    Returns (added, overflow) for the port (None for the reference harness)."""
+    offs, idx, img = pl if pl is not None else pairs(params, geom, P)
+    idx = np.ascontiguousarray(idx if len(idx) else np.zeros(1, np.int32), np.int32)
+    img = np.ascontiguousarray(img if len(img) else np.zeros(1, np.int8), np.int8)
+    s = P.struct()
+    if use_ref:
+        # the reference's loop body and fixBonds printf per neighbour: send the
+        # process's stdout to /dev/null around the call
+        libc = C.CDLL(None)
+        libc.fflush(None)
+        saved = os.dup(1)
+        null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(null, 1)
+        try:
+            rc = reflib().ref_init_bonds(C.byref(params), C.byref(geom), C.byref(s), offs.ctypes.data_as(_i64),
+                                         idx.ctypes.data_as(_i32), img.ctypes.data_as(_i8), rlim)
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(null)
+        if rc != BMXG_OK:
+            raise RuntimeError(f"ref_init_bonds failed: {rc}")
+        return None
+    added = C.c_int64(0)
+    over = C.c_int64(0)
+    rc = lib().orc_init_bonds(C.byref(params), C.byref(geom), C.byref(s), offs.ctypes.data_as(_i64),
+                              idx.ctypes.data_as(_i32), img.ctypes.data_as(_i8), rlim, C.byref(added),
+                              C.byref(over))
+    if rc != BMXG_OK:
+        raise RuntimeError(f"orc_init_bonds failed: {rc}")
+    return added.value, over.value

@@ -9,7 +9,8 @@
 //     from the reference tree through the stand-in AMReX headers in shim/;
 //   * the body of the force-gather lambda, src/des/bmx_pc_interaction.cpp:174-278
 //   * the body of the update lambda,       src/des/bmx_pc_interaction.cpp:317-436
-//     (both cut out of the reference file by oracle/Makefile into _ref/ and
+//   * the body of the InitBonds lambda,    src/des/bmx_pc_interaction.cpp:577-626
+//     (cut out of the reference file by oracle/Makefile into _ref/ and
 //     #included below inside plain loops over i, i.e. the serial CPU build).
 // What is NOT the reference's code: the neighbour list and the periodic wrap
 // (AMReX, absent from the reference tree) come from the oracle port
@@ -219,6 +220,42 @@ void ref_update(const bmxg_geometry *geom, bmxg_particles *p, const double *fc_i
     }
     from_aos(parts, p);
     orc_wrap(geom, p);
+}
+
+// InitBonds with the reference's loop body (bmx_pc_interaction.cpp:577-626)
+// and fixBonds, serial over i.
+int ref_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_particles *p,
+                   const int64_t *offs, const int32_t *idx, const int8_t *img, double rlim_in)
+{
+    if (!prm || !geom || !p || !offs) return BMXG_ERR_ARG;
+    std::vector<RefParticle> parts;
+    to_aos(p, parts);
+    const std::vector<RefParticle> ghosts = parts;
+    std::vector<Real> fpar_vec = force_params(prm);
+    Real *fpar = &fpar_vec[0];
+    const int nrp = (int)p->n;
+    RefParticle *pstruct = parts.data();
+    const double lx = geom->prob_hi[0] - geom->prob_lo[0];
+    const double ly = geom->prob_hi[1] - geom->prob_lo[1];
+    struct {
+        const RefParticle *g;
+        const int64_t *o;
+        const int32_t *ix;
+        const int8_t *im;
+        double lx, ly;
+        NbrRange getNeighbors(int i) const
+        {
+            return NbrRange{NbrIter{g, ix, im, o[i], lx, ly}, NbrIter{g, ix, im, o[i + 1], lx, ly}};
+        }
+    } nbor_data{ghosts.data(), offs, idx, img, lx, ly};
+    constexpr Real small_number = 1.0e-15;
+    const Real rlim = rlim_in;
+    for (int i = 0; i < nrp; ++i) {
+#include "initbonds_body.inc"
+    }
+    (void)small_number;
+    from_aos(parts, p);
+    return BMXG_OK;
 }
 
 // Single-call entry points for unit tests.

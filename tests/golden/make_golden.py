@@ -20,6 +20,9 @@ Cases:
                  deck input_fungi), 100 steps
   colonies_small 4 colonies of uneven size, each stepped on its own
   min_distance   segment pairs hitting every branch of evaluateMinimumDistance
+  init_bonds     InitBonds (bmx_pc_interaction.cpp:500-626 + fixBonds) on 400
+                 rod segments with their bond tables cleared, a few tables
+                 holding an unrelated bond first, and 100 spheres mixed in
 """
 import math
 import os
@@ -226,9 +229,52 @@ def min_distance():
     print("min_distance:", len(E))
 
 
+BOND_TABLES = ("n_bnds", "seg_id1", "seg_id2", "site")
+
+
+def init_bonds():
+    w = configs.rod_trees(seed=21, ntrees=10, per_tree=40, lx=0.064, ly=0.064)
+    R = w.particles
+    for k in BOND_TABLES:
+        R[k][:] = 0
+    S = configs.sphere_colony(100, 0.064, 0.064, np.random.default_rng(23))
+    S["id"] = np.arange(R.n + 1, R.n + S.n + 1, dtype=np.int32)
+    P = Particles.concat([R, S])
+    P.rods = True
+    geom = configs.box_geometry(0.064, 0.064)
+    pl = O.pairs(w.params, geom, P)
+    # a prior, unrelated bond in the tables of segments that gain at most two
+    T = P.copy()
+    O.init_bonds(w.params, geom, T, pl)
+    pre = [i for i in range(R.n) if T["n_bnds"][i] <= 2][::17]
+    n = P.n
+    for i in pre:
+        P["n_bnds"][i] = 1
+        P["seg_id1"][i] = 999_999
+        P["seg_id2"][i] = 3
+        P["site"][i] = 2
+    Q = P.copy()
+    added, over = O.init_bonds(w.params, geom, Q, pl)
+    assert over == 0
+    ref = P.copy()
+    O.init_bonds(w.params, geom, ref, pl, use_ref=True)
+    for k in BOND_TABLES:
+        assert np.array_equal(ref[k], Q[k]), k
+    out = {"params": pvec(w.params), "lo": np.array(geom.prob_lo), "hi": np.array(geom.prob_hi),
+           "n_cell": np.array(geom.n_cell), "periodic": np.array(geom.is_periodic),
+           "rlim": np.array(O.RLIM), "added": np.array(added)}
+    for k, v in P.a.items():
+        out["in_" + k] = v.copy()
+    for k in BOND_TABLES:
+        out["out_" + k] = ref[k].copy()
+    np.savez_compressed(os.path.join(OUT, "init_bonds.npz"), **out)
+    print(f"init_bonds: n={n} added={added} prior={len(pre)}")
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.have_ref():
         sys.exit("reference harness not built (reference tree missing?)")
-    for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance):
+    for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance,
+              init_bonds):
         f()
