@@ -92,6 +92,18 @@ struct bmxg_ctx {
 
     bool vel32 = false;       // the last step's velocities are in the FP32F buffers
     int64_t step_count = 0;   // steps since set_state (FP32F re-sync schedule)
+
+    // FP32F neighbour list with a skin (k_list.cu)
+    int list_mode = 1;            // 1: FP32F sphere steps use the list where it is exact; 0: never
+    bool list_on = false;         // the steps being enqueued use the list
+    bool list_valid = false;      // the list and its frozen bins describe the state
+    bool bins_exact = true;       // bins of buffer `parity` are the reference's (list steps freeze them)
+    double rmax = 0.0;            // largest radius of the state
+    float skin_cur = 0.0f;        // skin of the list control block
+    ListCtl *h_lctl = nullptr;    // pinned copy of the control block
+    unsigned long long body_runs_seen = 0;  // list builds already counted as launches
+    bool capturing = false;       // enqueue_step runs inside a graph capture
+    cudaStream_t body_stream = nullptr;     // captures the bodies of conditional nodes
 };
 
 namespace {
@@ -161,6 +173,8 @@ void free_state(bmxg_ctx *ctx)
     ctx->ui = nullptr;
     ctx->uperm = nullptr;
     ctx->have_state = false;
+    ctx->list_valid = false;
+    ctx->bins_exact = true;
 }
 
 int grid_for(bmxg_ctx *ctx, const Shape &s, int64_t n)
@@ -288,6 +302,8 @@ int bmxg_create(const bmxg_params *params, int32_t ncolonies, const bmxg_geometr
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_cnt, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_lctl, sizeof(ListCtl));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->body_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         ctx->err = cudaGetErrorString(e);
         bmxg_destroy(ctx);
@@ -308,6 +324,8 @@ void bmxg_destroy(bmxg_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_state(ctx);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+    if (ctx->h_lctl) cudaFreeHost(ctx->h_lctl);
+    if (ctx->body_stream) cudaStreamDestroy(ctx->body_stream);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
@@ -321,6 +339,7 @@ int bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params)
     if (check_params(params)) return fail(ctx, BMXG_ERR_ARG, "non-finite force parameter");
     ctx->prm = *params;
     drop_graphs(ctx);
+    ctx->list_valid = false;
     if (ctx->have_state) {
         build_geoms(ctx);
         CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol,
@@ -372,6 +391,17 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     for (int64_t i = 0; i < n; ++i) {
         if (ct[i] != BMXG_YEAST && ct[i] != BMXG_FUNGI) return fail(ctx, BMXG_ERR_ARG, "cell_type must be 0 or 1");
         rods |= (ct[i] == BMXG_FUNGI);
+    }
+    double rmax = 0.0;  // decides whether the FP32F list is exact for this state
+    {
+        std::vector<double> rr;
+        const double *r = p->radius;
+        if (where == BMXG_DEVICE && n) {
+            rr.resize((size_t)n);
+            CK(cudaMemcpy(rr.data(), p->radius, sizeof(double) * n, cudaMemcpyDeviceToHost));
+            r = rr.data();
+        }
+        for (int64_t i = 0; i < n; ++i) rmax = (r[i] > rmax || r[i] != r[i]) ? r[i] : rmax;
     }
     if (rods && (!p->c_length || !p->theta || !p->phi || !p->area || !p->id || !p->cpu || !p->n_bnds ||
                  !p->seg_id1 || !p->seg_id2 || !p->site))
@@ -517,6 +547,9 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     ctx->vel32 = false;
     ctx->step_count = 0;
     ctx->parity = 0;
+    ctx->rmax = rmax;
+    ctx->list_valid = false;
+    ctx->bins_exact = true;
     ctx->d_adh = nullptr;  // per-particle adhesion must be given again for the new state
     free_adjoint(ctx);
     std::memset(&ctx->stats, 0, sizeof(ctx->stats));
@@ -607,8 +640,147 @@ namespace {
 
 // Enqueue one DEM step reading buffer a.  resync: the FP32F sphere step
 // re-derives every slot's offsets and bin from its FP64 position.
+// profiling mode: an event pair around the force kernel of this step
+void prof_events(bmxg_ctx *ctx, cudaEvent_t *k0, cudaEvent_t *k1)
+{
+    *k0 = *k1 = nullptr;
+    if (!ctx->profiling) return;
+    while (ctx->kev.size() < 2 * (ctx->kev_used + 1)) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) break;
+        ctx->kev.push_back(e);
+    }
+    if (ctx->kev.size() >= 2 * (ctx->kev_used + 1)) {
+        *k0 = ctx->kev[2 * ctx->kev_used];
+        *k1 = ctx->kev[2 * ctx->kev_used + 1];
+        ++ctx->kev_used;
+    }
+}
+
+// ---- FP32F neighbour list with a skin ---------------------------------------
+constexpr int kListMaxAge = 64;      // bounds the FP32 drift of the frozen-frame offsets
+constexpr int kListExactEvery = 8;   // builds between exact FP64 re-binnings
+
+// Skin of the list for the loaded state and parameters, or 0 where the list
+// would not reproduce the reference's pair set: the largest cutoff
+// 2 r_max + bw plus the skin must stay within the smallest bin width (so
+// that every pair inside the cutoff is a stencil pair whatever the bins),
+// and BMXCheckPair must hold for every stencil pair.
+float list_skin(const bmxg_ctx *ctx)
+{
+    if (ctx->S.has_rods || ctx->n == 0 || ctx->n >= (1LL << kNbrShift)) return 0.0f;
+    double skin = 1e300;
+    for (const DevGeom &g : ctx->h_geoms) {
+        if (!g.nbh_trivial) return 0.0f;
+        const double dmin = std::min(g.dx[0], std::min(g.dx[1], g.dx[2]));
+        const double rcut = 2.0 * ctx->rmax + ctx->prm.bndry_width;
+        const double sk = std::min(0.25 * dmin, 0.95 * (dmin - rcut));
+        if (!(sk >= 0.02 * dmin)) return 0.0f;
+        skin = std::min(skin, sk);
+    }
+    return (float)skin;
+}
+
+// Allocate the list on first use; (re)initialise its control block when the
+// state or the skin changed, asking the next step for a build.
+int ensure_list(bmxg_ctx *ctx, float skin)
+{
+    DevState &S = ctx->S;
+    if (!S.nbr) {
+        int rc;
+        if ((rc = dalloc(ctx, &S.nbr, (size_t)kNbrCap * ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.ncnt, ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.lctl, 1))) return rc;
+        ctx->list_valid = false;
+        drop_graphs(ctx);  // captured kernels hold the state's pointers by value
+    }
+    if (ctx->list_valid && skin == ctx->skin_cur) return BMXG_OK;
+    double dmax = 0.0;
+    for (const DevGeom &g : ctx->h_geoms) dmax = std::max(dmax, std::max(g.dx[0], std::max(g.dx[1], g.dx[2])));
+    ListCtl h;
+    std::memset(&h, 0, sizeof(h));
+    h.skin = skin;
+    h.eps_step = (float)(4.0e-7 * dmax);
+    h.max_age = kListMaxAge;
+    h.force = 1;
+    h.exact_every = kListExactEvery;
+    CK(cudaMemcpyAsync(S.lctl, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->skin_cur = skin;
+    ctx->body_runs_seen = 0;
+    ctx->list_valid = true;
+    return BMXG_OK;
+}
+
+// Bins of buffer `parity` as the reference has them (after list steps froze
+// them); every consumer of the bins other than a list step calls this.
+int ensure_exact(bmxg_ctx *ctx)
+{
+    if (ctx->bins_exact || !ctx->have_state) return BMXG_OK;
+    const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, ctx->n);
+    LAUNCH(launch_bin(ctx->S, ctx->parity, grd, blk, ctx->stream));
+    LAUNCH(launch_rebuild(ctx->S, ctx->parity, ctx->scan_scratch, grd, blk, ctx->stream));
+    ctx->bins_exact = true;
+    ctx->list_valid = false;
+    return BMXG_OK;
+}
+
+// One FP32F list step: decide, build when needed (a conditional node when
+// capturing), then the force / update kernel.  Build kernels are counted as
+// launches only when they run (ListCtl::body_runs).
+int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
+{
+    const DevState &S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    const DevParams P = dev_params(ctx->prm);
+    CK(cudaMemsetAsync(ctx->d_cnt, 0, offsetof(DevCounters, nonfinite), st));
+    CK(cudaMemsetAsync(&ctx->d_cnt->pairs, 0, sizeof(DevCounters) - offsetof(DevCounters, pairs), st));
+    const int64_t n = ctx->n;
+    const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
+    if (ctx->capturing) {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *ed = nullptr;
+        size_t nd = 0;
+        CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &ed, &nd));
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+        LAUNCH(launch_list_decide(S, (unsigned long long)h, 1, st));
+        CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &ed, &nd));
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn = nullptr;
+        CK(cudaGraphAddNode(&cn, cg, deps, ed, nd, &cp));
+        CK(cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+        CK(cudaStreamBeginCaptureToGraph(ctx->body_stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeRelaxed));
+        launch_list_rebuild(S, P, a, ctx->scan_scratch, mgrd, mblk, ctx->body_stream);
+        const cudaError_t e1 = cudaPeekAtLastError();
+        cudaGraph_t body = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(ctx->body_stream, &body);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            return fail(ctx, BMXG_ERR_CUDA,
+                        std::string("list build capture: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    } else {
+        LAUNCH(launch_list_decide(S, 0, 0, st));
+        launch_list_rebuild(S, P, a, ctx->scan_scratch, mgrd, mblk, st);
+        const cudaError_t e = cudaPeekAtLastError();
+        if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("list build: ") + cudaGetErrorString(e));
+    }
+    cudaEvent_t k0, k1;
+    prof_events(ctx, &k0, &k1);
+    if (k0) cudaEventRecord(k0, st);
+    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm * 8, 256, st));
+    if (k1) cudaEventRecord(k1, st);
+    return BMXG_OK;
+}
+
 int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
 {
+    if (ctx->list_on) return enqueue_list_step(ctx, dt, a);
     const DevState &S = ctx->S;
     cudaStream_t st = ctx->stream;
     const DevParams P = dev_params(ctx->prm);
@@ -618,20 +790,8 @@ int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
     cudaMemsetAsync(&ctx->d_cnt->pairs, 0, sizeof(DevCounters) - offsetof(DevCounters, pairs), st);
     const int64_t n = ctx->n;
     const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
-    // profiling mode: an event pair around the force kernel of this step
-    cudaEvent_t k0 = nullptr, k1 = nullptr;
-    if (ctx->profiling) {
-        while (ctx->kev.size() < 2 * (ctx->kev_used + 1)) {
-            cudaEvent_t e;
-            if (cudaEventCreate(&e) != cudaSuccess) break;
-            ctx->kev.push_back(e);
-        }
-        if (ctx->kev.size() >= 2 * (ctx->kev_used + 1)) {
-            k0 = ctx->kev[2 * ctx->kev_used];
-            k1 = ctx->kev[2 * ctx->kev_used + 1];
-            ++ctx->kev_used;
-        }
-    }
+    cudaEvent_t k0, k1;
+    prof_events(ctx, &k0, &k1);
     if (!S.has_rods) {
         const Shape &sh = ctx->sh_sphere[precision == BMXG_FP32F ? 1 : 0];
         if (k0) cudaEventRecord(k0, st);
@@ -663,7 +823,9 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
     const int64_t before = ctx->launches;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc2 = BMXG_OK;
+    ctx->capturing = true;
     for (int s = 0; s < kResyncEvery && !rc2; ++s) rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == 0);
+    ctx->capturing = false;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc2) {
         if (g) cudaGraphDestroy(g);
@@ -697,6 +859,17 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     // nsubsteps = ceil(dt / dtsolid) with dtsolid := dt, subdt = dt / nsubsteps
     // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
     const double subdt = dt / 1.0;
+    // FP32F spheres use the neighbour list wherever it reproduces the pair set
+    const float skin = (precision == BMXG_FP32F && ctx->list_mode) ? list_skin(ctx) : 0.0f;
+    if (skin > 0.0f) {
+        int rc = ensure_list(ctx, skin);
+        if (rc) return rc;
+    } else {
+        int rc = ensure_exact(ctx);
+        if (rc) return rc;
+    }
+    if ((skin > 0.0f) != ctx->list_on) drop_graphs(ctx);
+    ctx->list_on = skin > 0.0f;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int32_t left = nsteps;
     ctx->kev_used = 0;
@@ -736,7 +909,19 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->list_on)
+        CK(cudaMemcpyAsync(ctx->h_lctl, ctx->S.lctl, sizeof(ListCtl), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->list_on) {
+        const unsigned long long runs = ctx->h_lctl->body_runs - ctx->body_runs_seen;
+        ctx->body_runs_seen = ctx->h_lctl->body_runs;
+        ctx->launches += (int64_t)runs * kListBodyKernels;
+        ctx->stats.n_rebins += (int64_t)runs;
+        ctx->bins_exact = false;
+    } else {
+        ctx->stats.n_rebins += nsteps;
+        ctx->list_valid = false;
+    }
     ctx->stepped = true;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
@@ -753,7 +938,6 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     ctx->stats.n_out_of_domain = (int64_t)ctx->h_cnt->out_of_domain;
     ctx->stats.n_edge_ghost = (int64_t)ctx->h_cnt->edge_ghost;
     ctx->stats.n_bond_repairs = (int64_t)ctx->h_cnt->bond_repairs;
-    ctx->stats.n_rebins += nsteps;
     if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
     return BMXG_OK;
 }
@@ -798,6 +982,7 @@ int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int6
     offs[0] = 0;
     *total = 0;
     if (n == 0) return BMXG_OK;
+    if (int rc0 = ensure_exact(ctx)) return rc0;
     cudaStream_t st = ctx->stream;
     const DevParams P = dev_params(ctx->prm);
     int64_t *d_offs = nullptr;
@@ -840,6 +1025,18 @@ int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int6
     return BMXG_OK;
 }
 
+int bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (mode != 0 && mode != 1) return fail(ctx, BMXG_ERR_ARG, "list mode must be 0 or 1");
+    if (ctx->list_mode != mode) {
+        ctx->list_mode = mode;
+        ctx->list_valid = false;
+        drop_graphs(ctx);
+    }
+    return BMXG_OK;
+}
+
 int bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow)
 {
     if (!ctx) return BMXG_ERR_ARG;
@@ -849,6 +1046,7 @@ int bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflo
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (!(rlim > 0.0)) rlim = 1.0e-7;
     if (ctx->n == 0 || !ctx->S.has_rods) return BMXG_OK;
+    if (int rc0 = ensure_exact(ctx)) return rc0;
     cudaStream_t st = ctx->stream;
     const DevParams P = dev_params(ctx->prm);
     unsigned long long *d_cnt = nullptr;
@@ -877,6 +1075,8 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (ctx->n == 0 || ctx->S.has_rods) return BMXG_OK;
+    if (int rc0 = ensure_exact(ctx)) return rc0;
+    ctx->list_valid = false;  // the sweep writes the other buffer
     const int64_t n = ctx->n;
     char devname[256] = {0};
     {
@@ -1072,6 +1272,8 @@ int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
     if (ctx->S.has_rods) return fail(ctx, BMXG_ERR_UNSUPPORTED, "the differentiation form covers spheres");
     if (nsteps < 0 || ckpt_every < 1 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt, nsteps or ckpt_every");
     (void)cudaGetLastError();
+    if (int rc0 = ensure_exact(ctx)) return rc0;
+    ctx->list_valid = false;
     const int64_t n = ctx->n;
     free_adjoint(ctx);
     if (n == 0) {
@@ -1123,6 +1325,7 @@ int bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0, double *dL
     cudaStream_t st = ctx->stream;
     const DevState &S = ctx->S;
     int rc;
+    ctx->list_valid = false;  // the recomputation rewrites buffer 0
     if (!ctx->lam[0]) {
         if ((rc = dalloc_adj(ctx, &ctx->lam[0], (size_t)3 * n))) return rc;
         if ((rc = dalloc_adj(ctx, &ctx->lam[1], (size_t)3 * n))) return rc;

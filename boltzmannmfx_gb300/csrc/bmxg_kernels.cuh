@@ -8,6 +8,29 @@
 
 namespace bmxg {
 
+// Control block of the FP32F neighbour list with a skin (k_list.cu).  The
+// list stays valid while no particle has moved more than skin / 2 since it
+// was built; acc bounds that displacement from above.
+struct ListCtl {
+    unsigned maxd2_bits;   // max over slots of |dt v|^2 in the last step (float bits, >= 0)
+    float acc;             // displacement bound since the last build
+    float skin;            // list skin (cm)
+    float eps_step;        // FP32 rounding of one position update, added per step
+    int age;               // steps since the last build
+    int max_age;           // rebuild at least this often (bounds FP32 offset drift)
+    int force;             // nonzero: rebuild at the next step (state changed)
+    int rebuild;           // this step's decision (read by the gated kernels)
+    int exact_every;       // every exact_every-th build re-bins from the FP64 positions
+    int exact_now;         // this build does (the others move frames in FP32)
+    int builds;            // builds decided so far
+    unsigned long long body_runs;  // builds actually run (counted by the first build kernel)
+    unsigned long long overflow;   // slots whose list exceeded the capacity (last build)
+};
+
+constexpr int kNbrCap = 32;          // list entries per slot (more: the slot walks its stencil)
+constexpr int kNbrShift = 26;        // entry = slot | (shift code << 26)
+constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
+
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
 // by the step parity a (read) / b = a ^ 1 (write).
 struct DevState {
@@ -49,6 +72,11 @@ struct DevState {
     int *position, *fix_site, *fflag, *sflag, *nflag;
     int *dltd;         // 6 planes
     double *fc;        // 6 planes, force gather of the rod path
+
+    // FP32F neighbour list with a skin (null unless the context is in list mode)
+    int *nbr;          // kNbrCap planes of n entries: neighbour slot | (dx, dy, dz bin shift + 1) << 26
+    int *ncnt;         // entries of each slot (may exceed kNbrCap)
+    ListCtl *lctl;
 };
 
 // Extension parameters of the differentiation form (k_adjoint.cu).
@@ -60,10 +88,14 @@ struct DiffParams {
 
 // ---- binning / counting sort (k_bin.cu) ----------------------------------
 int launch_bin(const DevState &S, int b, int grid, int block, cudaStream_t st);
-int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st);
+// gate (may be null): the kernels return at once when *gate == 0
+int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st, const int *gate = nullptr);
 size_t scan_scratch_ints(int n);
-int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st);
-int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st);
+// ra: buffer whose FP32 offsets the sorted copies take (default b)
+int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st, int ra = -1,
+                         const int *gate = nullptr);
+int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st,
+                   int ra = -1, const int *gate = nullptr);
 
 // caller-order staging -> slot order (set_state) and back (get_state)
 int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz,
@@ -90,6 +122,20 @@ int launch_pairs(const DevState &S, const DevParams &P, int a, int64_t *cnt_or_o
 // FP64 position this step
 int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision,
                         int grid, int block, cudaStream_t st, int resync = 1);
+
+// ---- FP32F neighbour list with a skin (k_list.cu) --------------------------
+// decide: fold the last step's displacement into the bound and decide
+// whether this step rebuilds; sets the graph conditional `cond` when use_cond
+int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond, cudaStream_t st);
+// rebuild (gated on lctl->rebuild): bins of buffer a's positions into the
+// list bins, column lists, and the list itself
+// (returns the kernels it enqueues, kListBodyKernels)
+int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_scratch, int grid, int block,
+                        cudaStream_t st);
+constexpr int kListBodyKernels = 7;
+// force + wall + update over the list, reading buffer a and writing buffer b
+int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block,
+                     cudaStream_t st);
 
 // ---- rods and mixed states (k_rod.cu) ------------------------------------
 int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st);

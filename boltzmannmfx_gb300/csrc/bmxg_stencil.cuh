@@ -117,24 +117,24 @@ __device__ __forceinline__ void col_to_bxy(const DevGeom &G, int col, int &bx, i
     by = q - (bx - 1) * G.n[1] + 1;
 }
 
-// Bin a slot at position (x, y, z) into buffer b: column, z bin, FP32
-// offsets from the bin corner, column count; flag out-of-domain z, images
-// that leave their halo cell, and non-finite positions.
-__device__ __forceinline__ void rebin_slot(const DevState &S, const DevGeom &G, int i, double x, double y,
-                                           double z, double r, int b)
+// Bin a slot at position (x, y, z): column and z bin into buffer bb, FP32
+// offsets from the bin corner into buffer rb, column count; flag
+// out-of-domain z, images that leave their halo cell, and non-finite positions.
+__device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom &G, int i, double x, double y,
+                                                double z, double r, int bb, int rb, bool count_domain = true)
 {
     const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
     const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
     const int bz = bin_of(z, G.plo[2], G.dxi[2], 1, G.n[2]);
     const int c = column_of(G, bx, by);
-    S.col[b][i] = c;
-    S.iz[b][i] = bz;
+    S.col[bb][i] = c;
+    S.iz[bb][i] = bz;
     const double cx = G.plo[0] + (double)(bx - 1) * G.dx[0];
     const double cy = G.plo[1] + (double)(by - 1) * G.dx[1];
     const double cz = G.plo[2] + (double)(bz - 1) * G.dx[2];
-    S.rel[b][i] = make_float4((float)(x - cx), (float)(y - cy), (float)(z - cz), (float)r);
+    S.rel[rb][i] = make_float4((float)(x - cx), (float)(y - cy), (float)(z - cz), (float)r);
     atomicAdd(&S.colcnt[c], 1);
-    if (!(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+    if (count_domain && !(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
     if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicAdd(&S.cnt->nonfinite, 1ULL);
     if (G.per[0] && (bx == 1 || bx == G.n[0])) {
         const int sx = (bx == 1) ? 1 : -1;
@@ -146,6 +146,13 @@ __device__ __forceinline__ void rebin_slot(const DevState &S, const DevGeom &G, 
         const int gb = bin_of(y + (double)sy * G.len[1], G.plo[1], G.dxi[1], 0, G.n[1] + 1);
         if (gb != (sy > 0 ? G.n[1] + 1 : 0)) atomicAdd(&S.cnt->edge_ghost, 1ULL);
     }
+}
+
+// Bin a slot into buffer b (bins and offsets).
+__device__ __forceinline__ void rebin_slot(const DevState &S, const DevGeom &G, int i, double x, double y,
+                                           double z, double r, int b)
+{
+    rebin_slot_into(S, G, i, x, y, z, r, b, b);
 }
 
 // Growth-surface cubic law of one site at height z
@@ -160,6 +167,30 @@ __device__ __forceinline__ double wall_law(double z, double rS, const DevParams 
     else v = 0.0;
     v -= P.z_g * P.z_k * rA * rA * rS;
     return v;
+}
+
+// Exact float -> double conversion with integer operations (GB300's FP64
+// pipe is the scarce resource here).  Subnormal floats flush to zero.
+__device__ __forceinline__ double f2d_int(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0u) return __longlong_as_double((long long)s);
+    const unsigned long long ee = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);  // 1023 - 127
+    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+    return __longlong_as_double((long long)(s | (ee << 52) | m));
+}
+
+// growth-surface cubic law in FP32 (bmx_cell_interaction_K.H:1019-1030)
+__device__ __forceinline__ float wall_law32(float dz, float rS, float zk, float zbw, float zg)
+{
+    const float rA = rS + zbw;
+    float v;
+    if (dz > 0.0f && dz < rA) v = -zk * (dz - rA) * (dz - rA) * (dz - rS);
+    else if (dz <= 0.0f) v = zk * rA * rA * rS;
+    else v = 0.0f;
+    return v - zg * zk * rA * rA * rS;
 }
 
 __device__ __forceinline__ const DevGeom &geom_of(const DevState &S, int i)

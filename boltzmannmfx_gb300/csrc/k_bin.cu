@@ -56,8 +56,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int &total)
     return before + x - v;
 }
 
-__global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ bsum)
+__global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ bsum, const int *gate)
 {
+    if (gate && !*gate) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int s = 0;
 #pragma unroll
@@ -68,8 +69,9 @@ __global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-__global__ void k_scan_top(int *bsum, int nb)
+__global__ void k_scan_top(int *bsum, int nb, const int *gate)
 {
+    if (gate && !*gate) return;
     int carry = 0;
     for (int base = 0; base < nb; base += kScanBlock) {
         const int k = base + threadIdx.x;
@@ -83,8 +85,9 @@ __global__ void k_scan_top(int *bsum, int nb)
 }
 
 __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__restrict__ bsum,
-                             int *__restrict__ out)
+                             int *__restrict__ out, const int *gate)
 {
+    if (gate && !*gate) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;
@@ -107,8 +110,9 @@ __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__res
 // Arrival order from the atomics is arbitrary; k_canon ranks every slot by
 // its (z bin, original index) key among the members of its column, which is
 // the order AMReX's serial binning gives (ascending index within a bin).
-__global__ void k_scatter(const DevState S, int b)
+__global__ void k_scatter(const DevState S, int b, const int *gate)
 {
+    if (gate && !*gate) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const int c = S.col[b][i];
         const int r = atomicSub(&S.colcnt[c], 1) - 1;  // leaves colcnt at zero
@@ -116,8 +120,9 @@ __global__ void k_scatter(const DevState S, int b)
     }
 }
 
-__global__ void k_canon(const DevState S, int b)
+__global__ void k_canon(const DevState S, int b, int ra, const int *gate)
 {
+    if (gate && !*gate) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const int c = S.col[b][i];
         const int s0 = S.colstart[b][c], s1 = S.colstart[b][c + 1];
@@ -131,7 +136,7 @@ __global__ void k_canon(const DevState S, int b)
         const int t = s0 + rank;
         S.perm[b][t] = i;
         if (S.srel[b]) {
-            S.srel[b][t] = S.rel[b][i];
+            S.srel[b][t] = S.rel[ra][i];
             S.siz[b][t] = izi;
             S.rank[b][i] = t;
         }
@@ -271,30 +276,31 @@ size_t scan_scratch_ints(int n)
     return (size_t)((n + kScanTile - 1) / kScanTile) + 2;
 }
 
-int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st)
+int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st, const int *gate)
 {
     const int nb = (n + kScanTile - 1) / kScanTile;
     if (nb == 0) {
         cudaMemsetAsync(out, 0, sizeof(int), st);
         return 0;
     }
-    k_scan_reduce<<<nb, kScanBlock, 0, st>>>(in, n, scratch);
-    k_scan_top<<<1, kScanBlock, 0, st>>>(scratch, nb);
-    k_scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, scratch, out);
+    k_scan_reduce<<<nb, kScanBlock, 0, st>>>(in, n, scratch, gate);
+    k_scan_top<<<1, kScanBlock, 0, st>>>(scratch, nb, gate);
+    k_scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, scratch, out, gate);
     return 3;
 }
 
-int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st)
+int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStream_t st, int ra, const int *gate)
 {
-    k_scatter<<<grid, block, 0, st>>>(S, b);
-    k_canon<<<grid, block, 0, st>>>(S, b);
+    k_scatter<<<grid, block, 0, st>>>(S, b, gate);
+    k_canon<<<grid, block, 0, st>>>(S, b, ra < 0 ? b : ra, gate);
     return 2;
 }
 
-int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st)
+int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st, int ra,
+                   const int *gate)
 {
-    int k = launch_scan(S.colcnt, S.colstart[b], S.ncols_total, scan_scratch, st);
-    return k + launch_scatter_canon(S, b, grid, block, st);
+    int k = launch_scan(S.colcnt, S.colstart[b], S.ncols_total, scan_scratch, st, gate);
+    return k + launch_scatter_canon(S, b, grid, block, st, ra, gate);
 }
 
 int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz, int *ucol,

@@ -109,30 +109,6 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
     }
 }
 
-// Exact float -> double conversion with integer operations (GB300's FP64
-// pipe is the scarce resource here).  Subnormal floats flush to zero.
-__device__ __forceinline__ double f2d_int(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
-    if (e == 0u) return __longlong_as_double((long long)s);
-    const unsigned long long ee = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);  // 1023 - 127
-    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
-    return __longlong_as_double((long long)(s | (ee << 52) | m));
-}
-
-// growth-surface cubic law in FP32 (bmx_cell_interaction_K.H:1019-1030)
-__device__ __forceinline__ float wall_law32(float dz, float rS, float zk, float zbw, float zg)
-{
-    const float rA = rS + zbw;
-    float v;
-    if (dz > 0.0f && dz < rA) v = -zk * (dz - rA) * (dz - rA) * (dz - rS);
-    else if (dz <= 0.0f) v = zk * rA * rA * rS;
-    else v = 0.0f;
-    return v - zg * zk * rA * rA * rS;
-}
-
 template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, double dt, int a,
                                                   int resync)

@@ -24,7 +24,8 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_set_stream", "bmxg_set_state", "bmxg_get_state", "bmxg_step",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
                "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
-               "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_autotune")
+               "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
+               "bmxg_autotune")
 
 
 class Ext(C.Structure):
@@ -69,6 +70,7 @@ def load_library(path=None):
                                  C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.bmxg_set_list_mode.argtypes = [vp, C.c_int32]
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
     L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
         [C.c_double, vp]
@@ -172,6 +174,10 @@ class Context:
                                             idx.ctypes.data_as(C.POINTER(C.c_int32)),
                                             img.ctypes.data_as(C.POINTER(C.c_int8)), cap, C.byref(total)))
         return offs, idx[:total.value], img[:total.value]
+
+    def set_list_mode(self, mode):
+        """1: FP32F sphere steps use the skin neighbour list where it is exact; 0: never."""
+        self._check(self.lib.bmxg_set_list_mode(self.h, int(mode)))
 
     def init_bonds(self, rlim=1.0e-7):
         """InitBonds on the loaded state (bond tables of coincident segment

@@ -135,7 +135,8 @@ typedef struct bmxg_stats {
     int64_t n_out_of_domain;    /* particles outside the non-periodic z range     */
     int64_t n_edge_ghost;       /* periodic images whose bin left the halo cell   */
     int64_t n_bond_repairs;     /* half-bonds repaired (rods)                      */
-    int64_t n_rebins;           /* steps whose bin order had to be rebuilt         */
+    int64_t n_rebins;           /* bin-order rebuilds: one per step, or one per
+                                   list build in the FP32F list mode (cumulative) */
     int64_t n_kernel_launches;  /* kernels this context enqueued, graph nodes counted */
     int64_t main_kernel_launches; /* force-kernel launches timed while profiling     */
     double  main_kernel_ms;     /* their summed device time (profiling mode)        */
@@ -300,6 +301,15 @@ int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *ge
 int  bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow);
 
 /* ---- tuning ------------------------------------------------------------- */
+
+/* FP32F sphere steps keep a neighbour list with a skin between builds when it
+ * reproduces the reference's pair set exactly: the largest force cutoff
+ * 2 r_max + bndry_width plus the skin fits inside the smallest bin width, and
+ * BMXCheckPair holds for every stencil pair.  mode 1 (default) uses it there,
+ * mode 0 never (every step re-bins and walks the stencil).  The reference
+ * rebuilds its AMReX neighbour list every step (bmx_pc_interaction.cpp:97-103);
+ * this switch has no counterpart there. */
+int  bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode);
 
 /* Time the launch shapes of the step kernels on the loaded state and keep
  * the fastest; results are cached in a JSON file at cache_path (may be NULL:

@@ -1,0 +1,172 @@
+"""FP32F neighbour list with a skin (k_list.cu) through the C ABI.
+
+The list mode must give the FP32F step of the per-step stencil path (the same
+pair set, FP32 rounding aside), hand exact reference bins back to every other
+consumer (FP64 steps, the pair-list export), stay out of the way where it would
+not be exact, and run the same steps eagerly as inside its CUDA graphs (with
+the build in a conditional node)."""
+import math
+
+import numpy as np
+import pytest
+
+from boltzmannmfx_gb300 import Context, configs
+from boltzmannmfx_gb300.abi import BMXG_FP32F, BMXG_FP64, Particles
+from common import relerr, same_pairs
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-5    # FP32F form, norm-wise relative force error
+
+
+def ctx_for(w, P=None, mode=1):
+    ctx = Context(w.params, w.geoms)
+    ctx.set_list_mode(mode)
+    ctx.set_state(w.particles if P is None else P, w.offsets)
+    return ctx
+
+
+def read(ctx, P):
+    Q = P.copy()
+    for k in ("velx", "vely", "velz"):
+        Q[k] = np.nan
+    ctx.get_state(Q)
+    return Q
+
+
+def vel(Q):
+    return np.stack([Q["velx"], Q["vely"], Q["velz"]])
+
+
+def periodic_disp(A, P, L):
+    d = A - P
+    return (d + L / 2) % L - L / 2
+
+
+def test_list_step_matches_stencil_path(gpu_lib, oracle_lib):
+    w = configs.sphere_fp32(n=40_000)
+    g = w.geoms[0]
+    A, B = ctx_for(w, mode=1), ctx_for(w, mode=0)
+    A.step(w.dt, 1, BMXG_FP32F)
+    B.step(w.dt, 1, BMXG_FP32F)
+    Pr = w.particles.copy()
+    fc = oracle_lib.forces(w.params, g, Pr, oracle_lib.pairs(w.params, g, Pr), nthreads=8)
+    assert relerr(vel(read(A, w.particles)), fc[:3]) <= TOL32
+    assert relerr(vel(read(A, w.particles)), vel(read(B, w.particles))) <= TOL32
+    A.step(w.dt, 39, BMXG_FP32F)
+    B.step(w.dt, 39, BMXG_FP32F)
+    sa, sb = A.stats(), B.stats()
+    assert 1 <= sa["n_rebins"] < 40 and sb["n_rebins"] == 40
+    QA, QB = read(A, w.particles), read(B, w.particles)
+    L = g.prob_hi[0] - g.prob_lo[0]
+    for k in ("x", "y"):
+        assert relerr(periodic_disp(QA[k], w.particles[k], L), periodic_disp(QB[k], w.particles[k], L)) <= 1e-4
+    assert relerr(QA["z"] - w.particles["z"], QB["z"] - w.particles["z"]) <= 1e-4
+    assert relerr(vel(QA), vel(QB)) <= 1e-4
+
+
+def test_exact_bins_after_list_steps(gpu_lib, oracle_lib):
+    """After list steps the pair export and an FP64 step are bit-exact to the
+    oracle on the positions the list steps produced."""
+    w = configs.sphere_fp32(n=40_000)
+    g = w.geoms[0]
+    ctx = ctx_for(w)
+    ctx.step(w.dt, 21, BMXG_FP32F)
+    P1 = read(ctx, w.particles)
+    assert same_pairs(ctx.pairs(), oracle_lib.pairs(w.params, g, P1))
+    Pr = P1.copy()
+    oracle_lib.step(w.params, g, Pr, w.dt, nthreads=8)
+    ctx.step(w.dt, 1, BMXG_FP64)
+    Q = read(ctx, w.particles)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(Q[k], Pr[k]), k
+    # and back to list steps from the FP64 state
+    ctx.step(w.dt, 3, BMXG_FP32F)
+    assert np.isfinite(read(ctx, w.particles)["x"]).all()
+
+
+def test_graph_and_eager_steps_agree(gpu_lib):
+    """The conditional-node graphs and the eager gated launches run the same
+    steps: bit-identical states."""
+    w = configs.sphere_fp32(n=20_000)
+    A, B = ctx_for(w), ctx_for(w)
+    B.set_profiling(True)   # every step eager
+    l0 = A.stats()["n_kernel_launches"]
+    A.step(w.dt, 24, BMXG_FP32F)
+    sa = A.stats()
+    B.step(w.dt, 24, BMXG_FP32F)
+    sb = B.stats()
+    # two kernels per step, seven per build
+    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 7 * sa["n_rebins"]
+    assert sa["n_rebins"] == sb["n_rebins"]
+    QA, QB = read(A, w.particles), read(B, w.particles)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(QA[k], QB[k]), k
+
+
+def test_list_overflow_walks_the_stencil(gpu_lib, oracle_lib):
+    """A particle with more list entries than the capacity falls back to a
+    stencil walk; its force is still the reference's."""
+    rng = np.random.default_rng(5)
+    lx = 0.032
+    bg = configs.sphere_colony(400, lx, lx, rng)
+    k = 60
+    c = np.array([0.016, 0.016, 0.046])
+    u = rng.normal(size=(k, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    pts = c + u * rng.uniform(2e-4, 9e-4, size=(k, 1))
+    cl = Particles(k)
+    cl["x"], cl["y"], cl["z"] = pts[:, 0], pts[:, 1], pts[:, 2]
+    cl["radius"] = 5.0e-4
+    cl["area"] = 4.0 * math.pi * 5.0e-4 ** 2
+    P = Particles.concat([bg, cl])
+    prm = configs.deck_params()
+    g = configs.box_geometry(lx, lx)
+    w = configs.Workload("cluster", prm, [g], P, np.array([0, P.n], np.int64), 0.25, 1)
+    A = ctx_for(w)
+    A.step(w.dt, 1, BMXG_FP32F)
+    Pr = P.copy()
+    fc = oracle_lib.forces(prm, g, Pr, oracle_lib.pairs(prm, g, Pr))
+    assert relerr(vel(read(A, P)), fc[:3]) <= TOL32
+
+
+def test_list_off_where_not_exact(gpu_lib):
+    """Radii whose cutoff reaches past a bin keep the per-step stencil path:
+    both modes give bit-identical results and re-bin every step."""
+    rng = np.random.default_rng(9)
+    P = configs.sphere_colony(3000, 0.064, 0.064, rng, rmin=9.0e-4, rmax=9.6e-4)
+    prm = configs.deck_params()
+    g = configs.box_geometry(0.064, 0.064)
+    w = configs.Workload("big", prm, [g], P, np.array([0, P.n], np.int64), 0.25, 5)
+    A, B = ctx_for(w, mode=1), ctx_for(w, mode=0)
+    A.step(w.dt, 5, BMXG_FP32F)
+    B.step(w.dt, 5, BMXG_FP32F)
+    assert A.stats()["n_rebins"] == 5
+    QA, QB = read(A, P), read(B, P)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(QA[k], QB[k]), k
+
+
+def test_list_batched_colonies(gpu_lib, oracle_lib):
+    """Several colonies of uneven size: first-step forces against the FP64
+    oracle per colony, and agreement with the stencil path over 30 steps."""
+    rng = np.random.default_rng(3)
+    sizes = [50, 4000, 12000, 137]
+    parts = [configs.sphere_colony(k, 0.128, 0.128, rng) for k in sizes]
+    P = Particles.concat(parts)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    prm = configs.deck_params()
+    g = configs.box_geometry(0.128, 0.128)
+    w = configs.Workload("cols", prm, [g] * len(sizes), P, off, 0.25, 30)
+    A, B = ctx_for(w, mode=1), ctx_for(w, mode=0)
+    A.step(w.dt, 1, BMXG_FP32F)
+    QA = read(A, P)
+    for c, Pc in enumerate(parts):
+        fc = oracle_lib.forces(prm, g, Pc.copy(), oracle_lib.pairs(prm, g, Pc))
+        assert relerr(vel(QA)[:, off[c]:off[c + 1]], fc[:3]) <= TOL32, c
+    B.step(w.dt, 1, BMXG_FP32F)
+    A.step(w.dt, 29, BMXG_FP32F)
+    B.step(w.dt, 29, BMXG_FP32F)
+    QA, QB = read(A, P), read(B, P)
+    assert relerr(vel(QA), vel(QB)) <= 1e-4
+    assert relerr(QA["z"] - P["z"], QB["z"] - P["z"]) <= 1e-4
