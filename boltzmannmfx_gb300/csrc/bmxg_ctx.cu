@@ -99,6 +99,8 @@ struct bmxg_ctx {
     bool list_valid = false;      // the list and its frozen bins describe the state
     bool bins_exact = true;       // bins of buffer `parity` are the reference's (list steps freeze them)
     double rmax = 0.0;            // largest radius of the state
+    int64_t ncells_total = 0;     // 3D cells over all colonies
+    int *cell_scratch = nullptr;  // scan scratch of the cell counts
     float skin_cur = 0.0f;        // skin of the list control block
     ListCtl *h_lctl = nullptr;    // pinned copy of the control block
     unsigned long long body_runs_seen = 0;  // list builds already counted as launches
@@ -169,6 +171,7 @@ void free_state(bmxg_ctx *ctx)
     ctx->S = DevState{};
     ctx->d_geoms = nullptr;
     ctx->scan_scratch = nullptr;
+    ctx->cell_scratch = nullptr;
     ctx->ud = nullptr;
     ctx->ui = nullptr;
     ctx->uperm = nullptr;
@@ -230,6 +233,7 @@ void build_geoms(bmxg_ctx *ctx)
 {
     ctx->h_geoms.resize(ctx->ncol);
     int col_base = 0;
+    int64_t cell_base = 0;
     for (int c = 0; c < ctx->ncol; ++c) {
         const bmxg_geometry &g = ctx->geoms[c];
         DevGeom &G = ctx->h_geoms[c];
@@ -248,6 +252,8 @@ void build_geoms(bmxg_ctx *ctx)
         }
         G.col_base = col_base;
         col_base += G.n[0] * G.n[1];
+        G.cell_base = (int)std::min<int64_t>(cell_base, INT32_MAX);
+        cell_base += (int64_t)G.n[0] * G.n[1] * G.n[2];
         G.slot_base = (int)ctx->offsets[c];
         G.slot_end = (int)ctx->offsets[c + 1];
         // two bins apart at most per axis: |r|^2 < 4 (dx^2 + dy^2 + dz^2)
@@ -263,6 +269,7 @@ void build_geoms(bmxg_ctx *ctx)
             G.wz[bz] = make_float2(hi, (float)(h - (double)hi));
         }
     }
+    ctx->ncells_total = cell_base;
 }
 
 }  // namespace
@@ -669,9 +676,10 @@ constexpr int kListExactEvery = 8;   // builds between exact FP64 re-binnings
 float list_skin(const bmxg_ctx *ctx)
 {
     if (ctx->S.has_rods || ctx->n == 0 || ctx->n >= (1LL << kNbrShift)) return 0.0f;
+    if (ctx->ncells_total >= (1LL << 30)) return 0.0f;  // 3D cell offsets of the build
     double skin = 1e300;
     for (const DevGeom &g : ctx->h_geoms) {
-        if (!g.nbh_trivial) return 0.0f;
+        if (!g.nbh_trivial || g.n[2] > 0xffff) return 0.0f;
         const double dmin = std::min(g.dx[0], std::min(g.dx[1], g.dx[2]));
         const double rcut = 2.0 * ctx->rmax + ctx->prm.bndry_width;
         const double sk = std::min(0.25 * dmin, 0.95 * (dmin - rcut));
@@ -689,8 +697,13 @@ int ensure_list(bmxg_ctx *ctx, float skin)
     if (!S.nbr) {
         int rc;
         if ((rc = dalloc(ctx, &S.nbr, (size_t)kNbrCap * ctx->n))) return rc;
-        if ((rc = dalloc(ctx, &S.ncnt, ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.lmeta, ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.cellcnt, ctx->ncells_total))) return rc;
+        if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
+        if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints((int)ctx->ncells_total)))) return rc;
         if ((rc = dalloc(ctx, &S.lctl, 1))) return rc;
+        S.ncells_total = (int)ctx->ncells_total;
+        CK(cudaMemsetAsync(S.cellcnt, 0, sizeof(int) * ctx->ncells_total, ctx->stream));
         ctx->list_valid = false;
         drop_graphs(ctx);  // captured kernels hold the state's pointers by value
     }
@@ -757,7 +770,7 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
         CK(cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
         CK(cudaStreamBeginCaptureToGraph(ctx->body_stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                          cudaStreamCaptureModeRelaxed));
-        launch_list_rebuild(S, P, a, ctx->scan_scratch, mgrd, mblk, ctx->body_stream);
+        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->body_stream);
         const cudaError_t e1 = cudaPeekAtLastError();
         cudaGraph_t body = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(ctx->body_stream, &body);
@@ -766,14 +779,14 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
                         std::string("list build capture: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     } else {
         LAUNCH(launch_list_decide(S, 0, 0, st));
-        launch_list_rebuild(S, P, a, ctx->scan_scratch, mgrd, mblk, st);
+        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, st);
         const cudaError_t e = cudaPeekAtLastError();
         if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("list build: ") + cudaGetErrorString(e));
     }
     cudaEvent_t k0, k1;
     prof_events(ctx, &k0, &k1);
     if (k0) cudaEventRecord(k0, st);
-    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm * 8, 256, st));
+    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, 256, st));
     if (k1) cudaEventRecord(k1, st);
     return BMXG_OK;
 }
@@ -938,6 +951,7 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     ctx->stats.n_out_of_domain = (int64_t)ctx->h_cnt->out_of_domain;
     ctx->stats.n_edge_ghost = (int64_t)ctx->h_cnt->edge_ghost;
     ctx->stats.n_bond_repairs = (int64_t)ctx->h_cnt->bond_repairs;
+    if (ctx->h_cnt->bad_index) return fail(ctx, BMXG_ERR_STATE, "internal: inconsistent bin counts");
     if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
     return BMXG_OK;
 }
@@ -1306,6 +1320,7 @@ int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
     ctx->traj_dt = subdt;
     ctx->vel32 = false;
     ctx->stats.n_kernel_launches = ctx->launches;
+    if (ctx->h_cnt->bad_index) return fail(ctx, BMXG_ERR_STATE, "internal: inconsistent bin counts");
     if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
     return BMXG_OK;
 }

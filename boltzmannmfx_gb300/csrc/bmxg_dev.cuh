@@ -39,6 +39,7 @@ struct DevGeom {
     int n[3];
     int per[3];
     int col_base;       // first global column of this colony
+    int cell_base;      // first global 3D cell (column-major, z fastest) of this colony
     int slot_base;      // first slot of this colony
     int slot_end;       // one past the last slot
     int nbh_trivial;    // 1: BMXCheckPair's r^2 <= neighborhood holds for every stencil pair
@@ -56,6 +57,7 @@ struct DevCounters {
     unsigned long long out_of_domain;
     unsigned long long edge_ghost;
     unsigned long long nonfinite;
+    unsigned long long bad_index;  // counting-sort slots outside 0..n-1 (skipped; an internal error, sticky)
     unsigned long long pairs;
     unsigned long long bond_repairs;
     unsigned long long moved;

@@ -75,7 +75,10 @@ struct DevState {
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
     int *nbr;          // kNbrCap planes of n entries: neighbour slot | (dx, dy, dz bin shift + 1) << 26
-    int *ncnt;         // entries of each slot (may exceed kNbrCap)
+    int *lmeta;        // per slot: z bin (bits 0-15), edge flags (16-18), list length (20-27, saturating)
+    int *cellcnt;      // per 3D cell counter, zero between uses
+    int *cellstart;    // ncells_total + 1 offsets of the cells in the sorted copies
+    int ncells_total;
     ListCtl *lctl;
 };
 

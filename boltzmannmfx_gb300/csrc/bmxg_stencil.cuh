@@ -121,7 +121,8 @@ __device__ __forceinline__ void col_to_bxy(const DevGeom &G, int col, int &bx, i
 // offsets from the bin corner into buffer rb, column count; flag
 // out-of-domain z, images that leave their halo cell, and non-finite positions.
 __device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom &G, int i, double x, double y,
-                                                double z, double r, int bb, int rb, bool count_domain = true)
+                                                double z, double r, int bb, int rb, bool count_domain = true,
+                                                bool count_col = true)
 {
     const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
     const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
@@ -133,7 +134,7 @@ __device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom
     const double cy = G.plo[1] + (double)(by - 1) * G.dx[1];
     const double cz = G.plo[2] + (double)(bz - 1) * G.dx[2];
     S.rel[rb][i] = make_float4((float)(x - cx), (float)(y - cy), (float)(z - cz), (float)r);
-    atomicAdd(&S.colcnt[c], 1);
+    if (count_col) atomicAdd(&S.colcnt[c], 1);
     if (count_domain && !(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
     if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicAdd(&S.cnt->nonfinite, 1ULL);
     if (G.per[0] && (bx == 1 || bx == G.n[0])) {

@@ -69,19 +69,23 @@ __global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
+// one block over the nb tile sums: each thread scans a contiguous segment
+// serially, one block-wide scan joins the segments
 __global__ void k_scan_top(int *bsum, int nb, const int *gate)
 {
     if (gate && !*gate) return;
-    int carry = 0;
-    for (int base = 0; base < nb; base += kScanBlock) {
-        const int k = base + threadIdx.x;
-        const int v = (k < nb) ? bsum[k] : 0;
-        int total;
-        const int ex = block_exclusive_scan(v, total);
-        if (k < nb) bsum[k] = carry + ex;
-        carry += total;
+    const int seg = (nb + kScanBlock - 1) / kScanBlock;
+    const int b0 = min((int)threadIdx.x * seg, nb), b1 = min(b0 + seg, nb);
+    int s = 0;
+    for (int k = b0; k < b1; ++k) s += bsum[k];
+    int total;
+    int run = block_exclusive_scan(s, total);
+    for (int k = b0; k < b1; ++k) {
+        const int v = bsum[k];
+        bsum[k] = run;
+        run += v;
     }
-    if (threadIdx.x == 0) bsum[nb] = carry;
+    if (threadIdx.x == 0) bsum[nb] = total;
 }
 
 __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__restrict__ bsum,
@@ -116,7 +120,9 @@ __global__ void k_scatter(const DevState S, int b, const int *gate)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const int c = S.col[b][i];
         const int r = atomicSub(&S.colcnt[c], 1) - 1;  // leaves colcnt at zero
-        S.tmp[S.colstart[b][c] + r] = i;
+        const int t = S.colstart[b][c] + r;
+        if (t >= 0 && t < S.n) S.tmp[t] = i;
+        else atomicAdd(&S.cnt->bad_index, 1ULL);
     }
 }
 
@@ -125,15 +131,19 @@ __global__ void k_canon(const DevState S, int b, int ra, const int *gate)
     if (gate && !*gate) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const int c = S.col[b][i];
-        const int s0 = S.colstart[b][c], s1 = S.colstart[b][c + 1];
+        const int s0 = max(S.colstart[b][c], 0), s1 = min(S.colstart[b][c + 1], S.n);
         const int izi = S.iz[b][i];
         const unsigned long long key = col_key(izi, S.orig[i]);
         int rank = 0;
         for (int t = s0; t < s1; ++t) {
             const int j = S.tmp[t];
-            rank += (col_key(S.iz[b][j], S.orig[j]) < key);
+            if ((unsigned)j < (unsigned)S.n) rank += (col_key(S.iz[b][j], S.orig[j]) < key);
         }
         const int t = s0 + rank;
+        if (t >= s1) {  // i is not among its column's members: inconsistent counts
+            atomicAdd(&S.cnt->bad_index, 1ULL);
+            continue;
+        }
         S.perm[b][t] = i;
         if (S.srel[b]) {
             S.srel[b][t] = S.rel[ra][i];

@@ -28,6 +28,8 @@
 // Roofline: the step kernel streams the slot state (FP64 positions in and
 // out, FP32 offsets in and out, FP32 velocities out) and the list; the
 // neighbour offsets it gathers are L2-resident.  HBM bound, no contraction.
+#include <algorithm>
+
 #include "bmxg_stencil.cuh"
 
 namespace bmxg {
@@ -40,14 +42,6 @@ constexpr unsigned kSlotMask = (1u << kNbrShift) - 1u;
 __device__ __forceinline__ float shift_of(unsigned c, float w)
 {
     return (c == 1u) ? 0.0f : ((c == 0u) ? -w : w);
-}
-
-// Order-preserving integer key of a double (-0 and +0 equal): the FP64
-// compares of the periodic wrap and the domain test without the FP64 pipe.
-__device__ __forceinline__ long long dkey(double v)
-{
-    const long long b = __double_as_longlong(v);
-    return (b >= 0) ? b : -(b & 0x7fffffffffffffffLL);
 }
 
 __global__ void k_list_decide(ListCtl *c, cudaGraphConditionalHandle h, int use_h)
@@ -90,11 +84,16 @@ __device__ __forceinline__ void reframe(float &r, int &b, float w, int nb, int p
     b = nbin;
 }
 
+__device__ __forceinline__ int cell_of(const DevGeom &G, int bx, int by, int bz)
+{
+    return G.cell_base + ((bx - 1) * G.n[1] + (by - 1)) * G.n[2] + (bz - 1);
+}
+
 // Bins of the list frames: every exact_every-th build (and the first) bins
 // buffer a's FP64 positions exactly and re-derives the FP32 offsets from
 // them (rebin_slot_into); the others move each frame by the bin its FP32
 // offset has reached, without FP64 arithmetic (GB300 issues FP64 at 1/64 of
-// the FP32 rate).  Either way the column counts are accumulated.
+// the FP32 rate).  Either way the 3D cell counts are accumulated.
 __global__ void k_list_rebin(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
@@ -103,28 +102,116 @@ __global__ void k_list_rebin(const DevState S, int a)
     if (blockIdx.x == 0 && threadIdx.x == 0) S.lctl->body_runs += 1ull;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, i);
+        int bx, by, bz;
         if (exact) {
-            rebin_slot_into(S, G, i, S.x[a][i], S.y[a][i], S.z[a][i], S.rad[i], B, a, false);
-            continue;
+            // (the column counters are the per-step paths'; the list counts cells)
+            rebin_slot_into(S, G, i, S.x[a][i], S.y[a][i], S.z[a][i], S.rad[i], B, a, false, false);
+            col_to_bxy(G, S.col[B][i], bx, by);
+            bz = S.iz[B][i];
+        } else {
+            float4 r = S.rel[a][i];
+            col_to_bxy(G, S.col[B][i], bx, by);
+            bz = S.iz[B][i];
+            reframe(r.x, bx, G.dxf[0], G.n[0], G.per[0]);
+            reframe(r.y, by, G.dxf[1], G.n[1], G.per[1]);
+            reframe(r.z, bz, G.dxf[2], G.n[2], 0);
+            S.col[B][i] = column_of(G, bx, by);
+            S.iz[B][i] = bz;
+            S.rel[a][i] = r;
         }
-        float4 r = S.rel[a][i];
-        int bx, by;
-        col_to_bxy(G, S.col[B][i], bx, by);
-        int bz = S.iz[B][i];
-        reframe(r.x, bx, G.dxf[0], G.n[0], G.per[0]);
-        reframe(r.y, by, G.dxf[1], G.n[1], G.per[1]);
-        reframe(r.z, bz, G.dxf[2], G.n[2], 0);
-        const int c = column_of(G, bx, by);
-        S.col[B][i] = c;
-        S.iz[B][i] = bz;
-        S.rel[a][i] = r;
-        atomicAdd(&S.colcnt[c], 1);
+        atomicAdd(&S.cellcnt[cell_of(G, bx, by, bz)], 1);
     }
 }
 
-// Walk every slot's stencil over the column-sorted copies (in sorted order,
-// so a warp's lanes share columns) and keep the pairs closer than
-// rA + skin (+ a slack covering the FP32 rounding of the test).
+// counting sort into the cells (arrival order from the atomics)
+__global__ void k_list_scatter(const DevState S)
+{
+    if (!S.lctl->rebuild) return;
+    constexpr int B = kListBins;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        int bx, by;
+        col_to_bxy(G, S.col[B][i], bx, by);
+        const int c = cell_of(G, bx, by, S.iz[B][i]);
+        const int r = atomicSub(&S.cellcnt[c], 1) - 1;  // leaves cellcnt at zero
+        const int t = S.cellstart[c] + r;
+        if (t >= 0 && t < S.n) S.tmp[t] = i;
+        else atomicAdd(&S.cnt->bad_index, 1ULL);
+    }
+}
+
+// deterministic order inside a cell (ascending original index), and the
+// sorted copies the build walks: offsets, z bin, slot, and each slot's rank
+__global__ void k_list_canon(const DevState S, int a)
+{
+    if (!S.lctl->rebuild) return;
+    constexpr int B = kListBins;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, i);
+        int bx, by;
+        col_to_bxy(G, S.col[B][i], bx, by);
+        const int bz = S.iz[B][i];
+        const int c = cell_of(G, bx, by, bz);
+        const int s0 = max(S.cellstart[c], 0), s1 = min(S.cellstart[c + 1], S.n);
+        const int oi = S.orig[i];
+        int rank = 0;
+        for (int t = s0; t < s1; ++t) {
+            const int j = S.tmp[t];
+            if ((unsigned)j < (unsigned)S.n) rank += (S.orig[j] < oi);
+        }
+        const int t = s0 + rank;
+        if (t >= s1) {  // i is not among its cell's members: inconsistent counts
+            atomicAdd(&S.cnt->bad_index, 1ULL);
+            continue;
+        }
+        S.perm[B][t] = i;
+        S.srel[B][t] = S.rel[a][i];
+        S.siz[B][t] = bz;
+        S.rank[B][i] = t;
+    }
+}
+
+// Visit the slots of the 3 x 3 neighbour columns of bin (bx, by), z bins
+// izi - 1 .. izi + 1 (periodic images included), as contiguous cell ranges
+// of the sorted copies.  f(u, dxs, dys, dzs): sorted position and the bin
+// shift of the neighbour relative to (bx, by, izi); the slot's own sorted
+// position self_t is skipped.  (One loop per column over its three z cells
+// keeps the lanes of a warp together better than a loop per cell.)
+template <class F>
+__device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G, int self_t, int bx, int by, int izi,
+                                            F &&f)
+{
+    constexpr int B = kListBins;
+    const int *__restrict__ cs = S.cellstart;
+    const int *__restrict__ siz = S.siz[B];
+    const int nz = G.n[2];
+    const int z0 = max(izi - 1, 1), z1 = min(izi + 1, nz);
+    for (int dxs = -1; dxs <= 1; ++dxs) {
+        int sx = bx + dxs;
+        if (sx < 1 || sx > G.n[0]) {
+            if (!G.per[0]) continue;
+            sx += (sx < 1) ? G.n[0] : -G.n[0];
+        }
+        for (int dys = -1; dys <= 1; ++dys) {
+            int sy = by + dys;
+            if (sy < 1 || sy > G.n[1]) {
+                if (!G.per[1]) continue;
+                sy += (sy < 1) ? G.n[1] : -G.n[1];
+            }
+            const int cb = G.cell_base + ((sx - 1) * G.n[1] + (sy - 1)) * nz;
+            const int hi = __ldg(&cs[cb + z1]);
+            for (int u = __ldg(&cs[cb + z0 - 1]); u < hi; ++u) {
+                if (u == self_t) continue;
+                f(u, dxs, dys, __ldg(&siz[u]) - izi);
+            }
+        }
+    }
+}
+
+// List build: every slot (in sorted order, so a warp's lanes share cells)
+// keeps the neighbours closer than rA + skin (+ a slack covering the FP32
+// rounding of the test), and its packed metadata: z bin, edge flags (x or y
+// bin on a periodic face, z bin at a closed face) and list length.
 __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevParams P)
 {
     if (!S.lctl->rebuild) return;
@@ -142,7 +229,7 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
         const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
         const float lim0 = reach + 4.0e-6f * fmaxf(dxb, fmaxf(dyb, dzb));
         int c = 0;
-        visit_sorted(S, G, B, t, bx, by, izi, [&](int u, int dxs, int dys, int dzs, int, int) {
+        visit_cells(S, G, t, bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
             const float4 q = __ldg(&S.srel[B][u]);
             const float ex = (me.x - q.x) - (float)dxs * dxb;
             const float ey = (me.y - q.y) - (float)dys * dyb;
@@ -154,26 +241,44 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
             if (c < kNbrCap) S.nbr[(size_t)c * n + i] = (int)((unsigned)__ldg(&S.perm[B][u]) | (code << kNbrShift));
             ++c;
         });
-        S.ncnt[i] = c;
+        const int edge = ((G.per[0] && (bx == 1 || bx == G.n[0])) ? 1 : 0) |
+                         ((G.per[1] && (by == 1 || by == G.n[1])) ? 2 : 0) | ((izi == 1 || izi == G.n[2]) ? 4 : 0);
+        S.lmeta[i] = izi | (edge << 16) | (min(c, 255) << 20);
         if (c > kNbrCap) ++over;
     }
     if (over) atomicAdd(&S.lctl->overflow, over);
 }
 
 // FP32F sphere step over the list: pair math and wall law in FP32 on the
-// frozen-frame offsets, FP64 position accumulation and periodic wrap.
-__global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevParams P, float dtf, int a)
+// frozen-frame offsets, FP64 position accumulation; the periodic wrap and
+// the domain test (FP64 compares) only run for slots whose frozen bin is on
+// a face, the only ones that can cross it before the next build.
+// Each block takes a contiguous chunk of slots (one wave of blocks covers
+// all slots), so a thread's colony changes rarely and is found by stepping
+// forward from the last one instead of a binary search per slot.
+// (256, 6): 40 registers, six blocks per SM; the kernel is latency bound and
+// gains more from the resident warps than it loses to the few spills
+__global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
 {
     constexpr int B = kListBins;
     const int b = a ^ 1;
     const int n = S.n;
     const float bwf = (float)P.bw, kf = (float)P.k;
     const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
+    const float4 *__restrict__ rel_a = S.rel[a];
+    const int *__restrict__ nbr = S.nbr;
     unsigned dmax = 0u;  // bits of the largest |dt v|^2 (non-negative floats order as integers)
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const DevGeom &G = geom_of(S, i);
-        const float4 me = S.rel[a][i];
-        const int izi = S.iz[B][i];
+    const int i0 = blockIdx.x * chunk;
+    const int i1 = min(i0 + chunk, n);
+    int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.geoms, S.ncol, i0 + threadIdx.x) : 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        while (colony + 1 < S.ncol && __ldg(&S.geoms[colony].slot_end) <= i) ++colony;
+        const DevGeom &G = S.geoms[colony];
+        const float4 me = rel_a[i];
+        const int meta = S.lmeta[i];
+        const int izi = meta & 0xffff;
+        const int edge = (meta >> 16) & 7;
+        const int cnt = meta >> 20;
         const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
         float gx = 0.0f, gy = 0.0f, gz = 0.0f;
         auto pair = [&](const float4 q, float ox, float oy, float oz) {
@@ -193,13 +298,12 @@ __global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevPa
             gy = __fmaf_rn(Fi, ey, gy);
             gz = __fmaf_rn(Fi, ez, gz);
         };
-        const int cnt = S.ncnt[i];
         if (cnt <= kNbrCap) {
             auto entry = [&](unsigned e, const float4 q) {
                 const unsigned code = e >> kNbrShift;
                 pair(q, shift_of(code & 3u, dxb), shift_of((code >> 2) & 3u, dyb), shift_of((code >> 4) & 3u, dzb));
             };
-            const int *col = S.nbr + i;
+            const int *col = nbr + i;
             int k = 0;
             // four entries in flight at a time: the list loads and the
             // neighbour gathers are independent across entries
@@ -208,10 +312,10 @@ __global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevPa
                 const unsigned e1 = (unsigned)__ldg(col + (size_t)(k + 1) * n);
                 const unsigned e2 = (unsigned)__ldg(col + (size_t)(k + 2) * n);
                 const unsigned e3 = (unsigned)__ldg(col + (size_t)(k + 3) * n);
-                const float4 q0 = __ldg(&S.rel[a][e0 & kSlotMask]);
-                const float4 q1 = __ldg(&S.rel[a][e1 & kSlotMask]);
-                const float4 q2 = __ldg(&S.rel[a][e2 & kSlotMask]);
-                const float4 q3 = __ldg(&S.rel[a][e3 & kSlotMask]);
+                const float4 q0 = __ldg(&rel_a[e0 & kSlotMask]);
+                const float4 q1 = __ldg(&rel_a[e1 & kSlotMask]);
+                const float4 q2 = __ldg(&rel_a[e2 & kSlotMask]);
+                const float4 q3 = __ldg(&rel_a[e3 & kSlotMask]);
                 entry(e0, q0);
                 entry(e1, q1);
                 entry(e2, q2);
@@ -219,12 +323,12 @@ __global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevPa
             }
             for (; k < cnt; ++k) {
                 const unsigned e = (unsigned)__ldg(col + (size_t)k * n);
-                entry(e, __ldg(&S.rel[a][e & kSlotMask]));
+                entry(e, __ldg(&rel_a[e & kSlotMask]));
             }
-        } else {  // list overflow: walk the frozen stencil with the current offsets
+        } else {  // list overflow: walk the frozen cells with the current offsets
             int bx, by;
             col_to_bxy(G, S.col[B][i], bx, by);
-            visit_sorted(S, G, B, S.rank[B][i], bx, by, izi, [&](int u, int dxs, int dys, int dzs, int, int) {
+            visit_cells(S, G, S.rank[B][i], bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
                 pair(__ldg(&S.rel[a][__ldg(&S.perm[B][u])]), (float)dxs * dxb, (float)dys * dyb,
                      (float)dzs * dzb);
             });
@@ -241,10 +345,11 @@ __global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevPa
         double nx = S.x[a][i] + f2d_int(ix);
         double ny = S.y[a][i] + f2d_int(iy);
         const double nz = S.z[a][i] + f2d_int(iz);
-        if (G.per[0] && (dkey(nx) < dkey(G.plo[0]) || dkey(nx) >= dkey(G.phi[0])))
-            nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
-        if (G.per[1] && (dkey(ny) < dkey(G.plo[1]) || dkey(ny) >= dkey(G.phi[1])))
-            ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+        if (edge) {
+            if (edge & 1) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
+            if (edge & 2) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+            if ((edge & 4) && !(nz >= G.plo[2] && nz < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+        }
         S.x[b][i] = nx;
         S.y[b][i] = ny;
         S.z[b][i] = nz;
@@ -252,7 +357,6 @@ __global__ void __launch_bounds__(256) k_list_step(const DevState S, const DevPa
         S.vxf[i] = vx;
         S.vyf[i] = vy;
         S.vzf[i] = vz;
-        if (dkey(nz) < dkey(G.plo[2]) || dkey(nz) >= dkey(G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
         const float d2 = __fmaf_rn(ix, ix, __fmaf_rn(iy, iy, __fmul_rn(iz, iz)));
         if (!isfinite(d2)) atomicAdd(&S.cnt->nonfinite, 1ULL);
         dmax = max(dmax, isfinite(d2) ? __float_as_uint(d2) : 0x7f800000u);
@@ -275,15 +379,23 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
 {
     const int *gate = &S.lctl->rebuild;
     k_list_rebin<<<grid, block, 0, st>>>(S, a);
-    int k = 1 + launch_rebuild(S, kListBins, scan_scratch, grid, block, st, a, gate);
+    int k = 1 + launch_scan(S.cellcnt, S.cellstart, S.ncells_total, scan_scratch, st, gate);
+    k_list_scatter<<<grid, block, 0, st>>>(S);
+    k_list_canon<<<grid, block, 0, st>>>(S, a);
     k_list_build<<<grid, block, 0, st>>>(S, P);
-    return k + 1;
+    return k + 3;
 }
 
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block,
                      cudaStream_t st)
 {
-    k_list_step<<<grid, block, 0, st>>>(S, P, (float)dt, a);
+    // grid = the SM count; one wave of resident blocks, each a chunk of slots
+    static int occ = 0;
+    if (occ == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_list_step, block, 0) != cudaSuccess) occ = 1;
+    const int want = grid * std::max(occ, 1);
+    int chunk = (S.n + want - 1) / want;
+    chunk = ((chunk + block - 1) / block) * block;
+    k_list_step<<<(S.n + chunk - 1) / chunk, block, 0, st>>>(S, P, (float)dt, a, chunk);
     return 1;
 }
 
