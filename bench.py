@@ -133,6 +133,47 @@ def ncu_traffic(key):
     return None
 
 
+def adjoint_cost(Context, configs, BMXG_FP64, nsteps=200, ckpt=20):
+    """The differentiation form on its configuration (20 000 spheres, 200
+    steps, checkpoint every 20, loss mean |x_T - target|^2, every extension
+    parameter on): device time of bmxg_forward, of bmxg_backward (reverse
+    sweep with checkpoint recomputation) and of the plain FP64 step, per step."""
+    w = configs.adjoint_spheres()
+    rng = np.random.default_rng(configs.SEED + 1)
+    adh = rng.uniform(0.0, 1.0e-3, w.n)
+    ctx = Context(w.params, w.geoms)
+    P = w.particles
+    target = np.stack([P["x"], P["y"], P["z"]]) + rng.normal(0.0, 1.0e-4, (3, w.n))
+
+    def fwd(T):
+        ctx.set_state(P)
+        ctx.set_ext(0.05, 1.0e-2, adh)
+        ctx.forward(w.dt, T, ckpt)
+        f_ms = ctx.stats()["last_step_ms"]
+        Q = P.copy()
+        ctx.get_state(Q, ("x", "y", "z"))
+        xT = np.stack([Q["x"], Q["y"], Q["z"]])
+        return f_ms, 2.0 * (xT - target) / w.n
+
+    _, g = fwd(ckpt)  # warm-up: compile-free, but first-touch allocations
+    ctx.backward(g)
+    f_ms, g = fwd(nsteps)
+    ctx.backward(g)
+    b_ms = ctx.stats()["last_step_ms"]
+    ctx.set_state(P)
+    ctx.set_ext(0.0, 0.0, None)
+    ctx.step(w.dt, 8, BMXG_FP64)
+    ctx.set_state(P)
+    ctx.step(w.dt, nsteps, BMXG_FP64)
+    p_ms = ctx.stats()["last_step_ms"]
+    ctx.close()
+    return {"workload": w.name, "particles": w.n, "steps": nsteps, "ckpt_every": ckpt,
+            "params": "positions, stiffness, damping, drag, per-particle adhesion",
+            "forward_ms_per_step": f_ms / nsteps, "adjoint_ms_per_step": b_ms / nsteps,
+            "plain_fp64_ms_per_step": p_ms / nsteps,
+            "adjoint_over_forward": b_ms / f_ms, "adjoint_over_plain_fp64": b_ms / p_ms}
+
+
 def cpu_baseline(w, budget_s=12.0):
     """Oracle (OpenMP over particles, all host threads) on a bounded sample of
     the workload: whole colonies until ~budget_s of CPU work."""
@@ -215,7 +256,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    from boltzmannmfx_gb300 import Context, build
+    from boltzmannmfx_gb300 import Context, build, configs
     from boltzmannmfx_gb300.abi import BMXG_FP32F, BMXG_FP64
     if rank == 0:
         build.build()
@@ -266,11 +307,15 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    l0 = ctx.stats()["n_kernel_launches"]
+    s0 = ctx.stats()
+    l0, r0 = s0["n_kernel_launches"], s0["n_rebins"]
     with ClockSampler(local) as clk:
         ms = timed_steps(prec, args.steps)
     torch.cuda.synchronize()
-    launches = ctx.stats()["n_kernel_launches"] - l0
+    s1 = ctx.stats()
+    launches = s1["n_kernel_launches"] - l0
+    rebins = s1["n_rebins"] - r0  # bin-order rebuilds: one per step, or one per list build
+    list_mode = kind == "sphere" and prec == BMXG_FP32F and rebins < args.steps
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -288,7 +333,10 @@ def run_ours(args):
     alg = ALG_BYTES[(kind, 1 if prec == BMXG_FP32F else 0)] * N
     peak, peak_kind = measured_peak()
     achieved = alg / (k_ms / 1e3) / 1e9
-    kname = ("k_sphere" if kind == "sphere" else "k_rod_force") + ("<FP32F>" if prec == BMXG_FP32F else "<FP64>")
+    if list_mode:
+        kname = "k_list_step"
+    else:
+        kname = ("k_sphere" if kind == "sphere" else "k_rod_force") + ("<FP32F>" if prec == BMXG_FP32F else "<FP64>")
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": peak_kind, "kernel_ms": k_ms,
             "algorithmic_bytes_per_launch": alg,
@@ -333,6 +381,10 @@ def run_ours(args):
            "h2d_bytes_per_step": int(H.nbytes(fin)), "d2h_bytes_per_step": int(H.nbytes(fout)),
            "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)"}
 
+    adj = None
+    if rank == 0 and w.name.startswith("colonies"):
+        adj = adjoint_cost(Context, configs, BMXG_FP64)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(w)
@@ -349,6 +401,14 @@ def run_ours(args):
                            "l2": ("L2 flushed between steps" if flush else
                                   f"inputs larger than L2 (state {state_bytes / 2**20:.0f} MiB)")},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "adjoint": adj,
+                "step_structure": ({"kind": "FP32F neighbour list with a skin", "list_builds": int(rebins),
+                                    "steps": args.steps,
+                                    "per_step": "k_list_decide + k_list_step",
+                                    "per_build": "k_list_rebin, 3 scan kernels, k_list_scatter, k_list_canon, "
+                                                 "k_list_build (CUDA-graph conditional node)"}
+                                   if list_mode else
+                                   {"kind": "per-step binning", "rebins": int(rebins), "steps": args.steps}),
                 "clocks": clk.summary(),
                 "other_form": {"form": "FP64" if other == BMXG_FP64 else "FP32F", "value": v_other,
                                "unit": UNIT, "ms_per_step": ms_other / args.steps},
