@@ -364,6 +364,10 @@ def run_ours(args):
     # end to end through the C ABI with pinned host buffers
     fin = ("x", "y", "z", "radius", "cell_type")
     fout = ("x", "y", "z", "velx", "vely", "velz")
+    if kind == "rod":  # segments: orientation, shape, identity and the bond table in; orientation out
+        fin += ("c_length", "theta", "phi", "area", "bond_scale", "id", "cpu", "n_bnds", "seg_id1", "seg_id2",
+                "site", "position", "fuse_tip", "fix_site")
+        fout += ("theta", "phi", "wx", "wy", "wz", "n_bnds", "seg_id1", "seg_id2", "site", "position")
     H = pinned_particles(w.particles, set(fin) | set(fout))
     ke = min(args.steps, 20)
     for _ in range(2):

@@ -26,8 +26,11 @@
 //    rounding, without two 3x3 tensor rotations per pair.
 //  * FP32F: contact pair math in FP32 on the FP64-differenced bin-relative
 //    offsets; pairs whose segments are near-parallel (det < 0.05 Aii Ajj,
-//    where the closest-point solve loses precision) and bonded pairs (a
-//    spring on the difference of two coincident end points) are done in FP64.
+//    where the closest-point solve loses precision), pairs whose closest
+//    points are within 1 % of the segment lengths (touching or crossing
+//    segments, where the separation's direction is end-point rounding noise)
+//    and bonded pairs (a spring on the difference of two coincident end
+//    points) are done in FP64.
 #include "bmxg_stencil.cuh"
 
 namespace bmxg {
@@ -126,7 +129,7 @@ __device__ void min_distance(const T *a1, const T *a2, const T *b1, const T *b2,
 // (bmx_cell_interaction_K.H:552-772).  Returns f1 (site 1) and f2 (site 2).
 template <class T>
 __device__ void rod_site_forces(const T *r12, const T *ni, T Li, const T *nj, T Lj, T rS, T rA, T k,
-                                int si, int sj, T kb, T *f1, T *f2)
+                                int si, int sj, T kb, T *f1, T *f2, T *r_out = nullptr)
 {
     T e1[3], e2[3], g1[3], g2[3];
     for (int d = 0; d < 3; ++d) {
@@ -149,6 +152,7 @@ __device__ void rod_site_forces(const T *r12, const T *ni, T Li, const T *nj, T 
     T dv[3];
     for (int d = 0; d < 3; ++d) dv[d] = (e1[d] + ti * (e2[d] - e1[d])) - (g1[d] + tj * (g2[d] - g1[d]));
     const T r = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    if (r_out) *r_out = r;
     // r <= 1e-8: the reference keeps the unnormalised separation (its
     // fallback direction goes to shadowing locals, :744-746); so do we.
     if (r > T(1.0e-8)) {
@@ -344,14 +348,19 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                     const float rij = nif[0] * njf[0] + nif[1] * njf[1] + nif[2] * njf[2];
                     const bool bonded = (si == 1 || si == 2) && (sj == 1 || sj == 2);
                     if (!bonded && 1.0f - rij * rij >= 0.05f) {
-                        float g1[3], g2[3];
+                        float g1[3], g2[3], rf;
                         rod_site_forces<float>(r12f, nif, (float)Li, njf, (float)Lj, (float)rS, (float)rA,
-                                               (float)P.k, si, sj, (float)kb, g1, g2);
-                        for (int k = 0; k < 3; ++k) {
-                            f1[k] = (double)g1[k];
-                            f2[k] = (double)g2[k];
+                                               (float)P.k, si, sj, (float)kb, g1, g2, &rf);
+                        // touching or crossing segments (closest points within 1 % of the
+                        // segment lengths): the direction of the FP32 separation is
+                        // rounding noise of the end points there, so such pairs go FP64
+                        if (rf >= 0.01f * (float)(Li + Lj)) {
+                            for (int k = 0; k < 3; ++k) {
+                                f1[k] = (double)g1[k];
+                                f2[k] = (double)g2[k];
+                            }
+                            done = true;
                         }
-                        done = true;
                     }
                 }
                 if (!done) {
