@@ -170,3 +170,21 @@ def test_list_batched_colonies(gpu_lib, oracle_lib):
     QA, QB = read(A, P), read(B, P)
     assert relerr(vel(QA), vel(QB)) <= 1e-4
     assert relerr(QA["z"] - P["z"], QB["z"] - P["z"]) <= 1e-4
+
+
+def test_position_accumulation_is_binary64(gpu_lib):
+    """The list step accumulates positions in FP64: the result equals
+    x + double(float(dt) * v) bit for bit (v the step's FP32 velocity)."""
+    w = configs.sphere_fp32(n=40_000)
+    g = w.geoms[0]
+    ctx = ctx_for(w)
+    ctx.step(w.dt, 1, BMXG_FP32F)
+    Q = read(ctx, w.particles)
+    dtf = np.float32(w.dt)
+    for k, v in (("x", "velx"), ("y", "vely"), ("z", "velz")):
+        inc = (dtf * Q[v].astype(np.float32)).astype(np.float64)
+        want = w.particles[k] + inc
+        ax = {"x": 0, "y": 1, "z": 2}[k]
+        inside = (want >= g.prob_lo[ax]) & (want < g.prob_hi[ax])  # not wrapped this step
+        assert inside.mean() > 0.99
+        assert np.array_equal(Q[k][inside], want[inside]), k
