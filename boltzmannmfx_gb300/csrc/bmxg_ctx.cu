@@ -714,6 +714,10 @@ int ensure_list(bmxg_ctx *ctx, float skin)
     std::memset(&h, 0, sizeof(h));
     h.skin = skin;
     h.eps_step = (float)(4.0e-7 * dmax);
+    for (int k = 0; k < 3; ++k) {  // empty spreads (see k_list_decide)
+        h.inc_min[k] = 0xff800000u;
+        h.inc_max[k] = 0x007fffffu;
+    }
     h.max_age = kListMaxAge;
     h.force = 1;
     h.exact_every = kListExactEvery;

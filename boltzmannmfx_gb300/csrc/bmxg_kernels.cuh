@@ -9,11 +9,16 @@
 namespace bmxg {
 
 // Control block of the FP32F neighbour list with a skin (k_list.cu).  The
-// list stays valid while no particle has moved more than skin / 2 since it
-// was built; acc bounds that displacement from above.
+// list stays valid while no pair's separation has changed by the skin since
+// it was built; acc bounds that change from above.
 struct ListCtl {
-    unsigned maxd2_bits;   // max over slots of |dt v|^2 in the last step (float bits, >= 0)
-    float acc;             // displacement bound since the last build
+    // per component, the smallest and largest position increment of the last
+    // step over all slots (order-preserving integer keys of the floats); the
+    // change of any pair's separation since the build is bounded per
+    // component by the sum over steps of (largest - smallest)
+    unsigned inc_min[3], inc_max[3];
+    float range[3];        // those sums since the last build
+    float acc;             // |range|: the bound on any pair's separation change
     float skin;            // list skin (cm)
     float eps_step;        // FP32 rounding of one position update, added per step
     int age;               // steps since the last build

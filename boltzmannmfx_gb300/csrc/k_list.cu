@@ -6,8 +6,8 @@
 // rA + skin is at most the smallest bin width, any pair that close sits in
 // neighbouring bins, so the reference's stencil list holds it whatever the
 // binning is.  The list built here holds every pair closer than rA + skin
-// at build time; while no particle has moved more than skin / 2 since, it
-// still holds every pair closer than rA.  The pair set of a step is
+// at build time; while no pair's separation has changed by the skin since,
+// it still holds every pair closer than rA.  The pair set of a step is
 // therefore the reference's; only the FP32 rounding of the pair math (the
 // precision form) differs from it.
 //
@@ -16,14 +16,14 @@
 // and wrap periodically every step as in the reference.  A build moves
 // every frame to the bin its offset has reached (every kListExactEvery-th
 // build re-bins exactly from the FP64 positions instead, which also bounds
-// the FP32 drift of the offsets), rebuilds the column lists and walks the
+// the FP32 drift of the offsets), rebuilds the cell lists and walks the
 // stencil once.  The bins need not be the reference's here: with
 // rA + skin within a bin width, any binning finds the same pairs.
-// k_list_decide folds each step's largest
-// displacement into a bound and asks for a build when the bound reaches
-// skin / 2 (or after max_age steps); inside a CUDA graph the build kernels
-// sit in a conditional node that the decision switches, so a step without
-// a build launches two kernels.
+// k_list_decide bounds the separation change of every pair from the spread
+// of each step's increments and asks for a build when the bound reaches the
+// skin (or after max_age steps); inside a CUDA graph the build kernels sit
+// in a conditional node that the decision switches, so a step without a
+// build launches two kernels.
 //
 // Roofline: the step kernel streams the slot state (FP64 positions in and
 // out, FP32 offsets in and out, FP32 velocities out) and the list; the
@@ -44,21 +44,55 @@ __device__ __forceinline__ float shift_of(unsigned c, float w)
     return (c == 1u) ? 0.0f : ((c == 0u) ? -w : w);
 }
 
+// Order-preserving unsigned key of a float (and back): atomicMin / atomicMax
+// on the keys order the floats.
+__device__ __forceinline__ unsigned fkey(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ float funkey(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+constexpr unsigned kKeyPosInf = 0xff800000u;  // fkey(+inf)
+constexpr unsigned kKeyNegInf = 0x007fffffu;  // fkey(-inf)
+
+// The bound: for any pair, the separation change since the build is, per
+// component, at most the sum over steps of the spread (largest minus
+// smallest) of that step's increments; its length at most the length of
+// those sums.  Unlike twice the largest displacement, it does not count a
+// drift common to all slots (here: the rise of the slots below the growth
+// surface).  Each step adds eps_step per component for the FP32 rounding of
+// the offset updates.
 __global__ void k_list_decide(ListCtl *c, cudaGraphConditionalHandle h, int use_h)
 {
-    const float m2 = __uint_as_float(c->maxd2_bits);
-    c->maxd2_bits = 0u;
-    const float acc = c->acc + sqrtf(m2) * 1.000001f + c->eps_step;
+    float r2 = 0.0f;
+    float rg[3];
+    for (int k = 0; k < 3; ++k) {
+        const unsigned lo = c->inc_min[k], hi = c->inc_max[k];
+        // no slot reported (empty state): no spread
+        const float spread = (hi >= lo) ? (funkey(hi) - funkey(lo)) : 0.0f;
+        rg[k] = c->range[k] + spread * 1.000001f + c->eps_step;
+        r2 += rg[k] * rg[k];
+        c->inc_min[k] = kKeyPosInf;
+        c->inc_max[k] = kKeyNegInf;
+    }
+    const float acc = sqrtf(r2);
     const int age = c->age + 1;
-    const bool rb = c->force != 0 || !(2.0f * acc <= c->skin) || age > c->max_age;
+    const bool rb = c->force != 0 || !(acc <= c->skin) || age > c->max_age;
     if (rb) {
         c->exact_now = (c->force != 0 || c->builds % c->exact_every == 0) ? 1 : 0;
+        for (int k = 0; k < 3; ++k) c->range[k] = 0.0f;
         c->acc = 0.0f;
         c->age = 0;
         c->force = 0;
         c->builds += 1;
         c->overflow = 0ull;
     } else {
+        for (int k = 0; k < 3; ++k) c->range[k] = rg[k];
         c->acc = acc;
         c->age = age;
     }
@@ -267,7 +301,8 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
     const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
     const float4 *__restrict__ rel_a = S.rel[a];
     const int *__restrict__ nbr = S.nbr;
-    unsigned dmax = 0u;  // bits of the largest |dt v|^2 (non-negative floats order as integers)
+    // smallest and largest increment per component (order-preserving keys)
+    unsigned kmin[3] = {kKeyPosInf, kKeyPosInf, kKeyPosInf}, kmax[3] = {kKeyNegInf, kKeyNegInf, kKeyNegInf};
     const int i0 = blockIdx.x * chunk;
     const int i1 = min(i0 + chunk, n);
     int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.geoms, S.ncol, i0 + threadIdx.x) : 0;
@@ -357,13 +392,33 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
         S.vxf[i] = vx;
         S.vyf[i] = vy;
         S.vzf[i] = vz;
-        const float d2 = __fmaf_rn(ix, ix, __fmaf_rn(iy, iy, __fmul_rn(iz, iz)));
-        if (!isfinite(d2)) atomicAdd(&S.cnt->nonfinite, 1ULL);
-        dmax = max(dmax, isfinite(d2) ? __float_as_uint(d2) : 0x7f800000u);
+        if (!isfinite(ix + iy + iz)) {
+            atomicAdd(&S.cnt->nonfinite, 1ULL);
+            kmin[0] = 0u;  // spreads the bound: the next step rebuilds
+            kmax[0] = 0xffffffffu;
+        }
+        const unsigned k0 = fkey(ix), k1 = fkey(iy), k2 = fkey(iz);
+        kmin[0] = min(kmin[0], k0);
+        kmax[0] = max(kmax[0], k0);
+        kmin[1] = min(kmin[1], k1);
+        kmax[1] = max(kmax[1], k1);
+        kmin[2] = min(kmin[2], k2);
+        kmax[2] = max(kmax[2], k2);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-    if ((threadIdx.x & 31) == 0 && dmax) atomicMax(&S.lctl->maxd2_bits, dmax);
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            kmin[k] = min(kmin[k], __shfl_xor_sync(0xffffffffu, kmin[k], o));
+            kmax[k] = max(kmax[k], __shfl_xor_sync(0xffffffffu, kmax[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0 && kmax[0] >= kmin[0]) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&S.lctl->inc_min[k], kmin[k]);
+            atomicMax(&S.lctl->inc_max[k], kmax[k]);
+        }
+    }
 }
 
 }  // namespace
