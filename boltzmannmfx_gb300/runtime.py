@@ -25,7 +25,8 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
                "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
-               "bmxg_autotune")
+               "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk", "bmxg_read_checkpoint",
+               "bmxg_io_last_error", "bmxg_autotune")
 
 
 class Ext(C.Structure):
@@ -71,6 +72,13 @@ def load_library(path=None):
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.bmxg_set_list_mode.argtypes = [vp, C.c_int32]
+    PS = C.POINTER(ParticlesStruct)
+    L.bmxg_read_ascii.argtypes = [C.c_char_p, PS, C.c_int64, C.POINTER(C.c_int64)]
+    L.bmxg_write_ascii.argtypes = [C.c_char_p, PS]
+    L.bmxg_write_vtk.argtypes = [C.c_char_p, PS, C.POINTER(C.c_double)]
+    L.bmxg_read_checkpoint.argtypes = [C.c_char_p, C.c_int32, PS, C.c_int64, C.POINTER(C.c_int64)]
+    L.bmxg_io_last_error.restype = C.c_char_p
+    L.bmxg_io_last_error.argtypes = []
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
     L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
         [C.c_double, vp]
@@ -216,3 +224,51 @@ class Context:
 
     def autotune(self, cache_path=None):
         self._check(self.lib.bmxg_autotune(self.h, cache_path.encode() if cache_path else None))
+
+
+# ---- fixture I/O (host functions of libbmxg.so; no device needed) -------------
+
+def _io_check(L, rc):
+    if rc != abi.BMXG_OK:
+        raise BmxgError(rc, L.bmxg_io_last_error().decode())
+
+
+def _two_call(read, *args):
+    """Count with a NULL buffer, then fill a Particles of that size."""
+    L = load_library()
+    n = C.c_int64(0)
+    rc = read(*args, None, 0, C.byref(n))
+    if rc not in (abi.BMXG_OK, abi.BMXG_ERR_CAPACITY):
+        _io_check(L, rc)
+    P = Particles(n.value, rods=True)
+    s = P.struct()
+    _io_check(L, read(*args, C.byref(s), n.value, C.byref(n)))
+    P.rods = bool((P["cell_type"] == abi.FUNGI).any())
+    return P
+
+
+def read_ascii(path):
+    """Particles of a particle input file of the reference
+    (BMXParticleContainer::InitParticlesAscii format)."""
+    L = load_library()
+    return _two_call(L.bmxg_read_ascii, os.fsencode(path))
+
+
+def write_ascii(path, P):
+    L = load_library()
+    _io_check(L, L.bmxg_write_ascii(os.fsencode(path), C.byref(P.struct())))
+
+
+def write_vtk(path, P, conc_b=None):
+    """Legacy-VTK polydata as BMXParticleContainer::WriteToAscii writes it."""
+    L = load_library()
+    c = None if conc_b is None else np.ascontiguousarray(conc_b, np.float64)
+    cp = c.ctypes.data_as(C.POINTER(C.c_double)) if c is not None else None
+    _io_check(L, L.bmxg_write_vtk(os.fsencode(path), C.byref(P.struct()), cp))
+
+
+def read_checkpoint(particles_dir, level=-1):
+    """Particles of an AMReX checkpoint (Version_Two_Dot_One_double);
+    particles_dir is the checkpoint's `particles` directory."""
+    L = load_library()
+    return _two_call(L.bmxg_read_checkpoint, os.fsencode(particles_dir), int(level))

@@ -300,6 +300,42 @@ int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *ge
  * here they are dropped and the call returns BMXG_ERR_CAPACITY. */
 int  bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow);
 
+/* ---- fixture I/O (host only; no context, no device) ---------------------- */
+
+/* Particle input file of BMXParticleContainer::InitParticlesAscii
+ * (src/des/bmx_pc_init.cpp:17-132): the count, then 27 values per particle
+ * (x y z radius c_length theta phi area vol velx vely velz wx wy wz fx fy fz
+ * taux tauy tauz gx gy gz dadt dvdt cell_type), read as one stream.  Fields
+ * the file does not carry get the reference's values (id = 1..n, cpu = 0,
+ * bond_scale = 1, no bonds).  Call with out == NULL (or cap too small) to
+ * get the count in *n (BMXG_ERR_CAPACITY); then with out->n == *n.  Only the
+ * non-NULL arrays of out are filled. */
+int  bmxg_read_ascii(const char *path, bmxg_particles *out, int64_t cap, int64_t *n);
+
+/* The same format written from a state (vol from the shape; force, torque,
+ * gradient and rates as 0), 17 significant digits: bmxg_read_ascii reads
+ * back the same doubles.  The reference has no writer for this format. */
+int  bmxg_write_ascii(const char *path, const bmxg_particles *p);
+
+/* Legacy-VTK polydata of BMXParticleContainer::WriteToAscii
+ * (src/des/bmx_pc_write.cpp:11-219): segment end points pos +- L/2 n, one
+ * polygon per particle, the particle index as scalar and conc_b (may be
+ * NULL: 0) as the "conc_B" scalar of both end points. */
+int  bmxg_write_vtk(const char *path, const bmxg_particles *p, const double *conc_b);
+
+/* Particles of an AMReX checkpoint in the Version_Two_Dot_One_double format
+ * (dir = .../chkNNNNN/particles; written by bmx::WriteCheckPointFile,
+ * src/io/bmx_chk.cpp:114-160, read back by bmx::Restart,
+ * src/io/bmx_restart.cpp:24-225), all grids of `level` (-1: every level).
+ * Component layouts: the current realIdx/intIdx (34 real, 35 int) and the
+ * 33 + 33 layout of the checkpoints shipped in exec/ (realIdx without
+ * bond_scale, intIdx without fuse_tip and fix_site; those get 1 and 0).
+ * Two-call protocol as bmxg_read_ascii. */
+int  bmxg_read_checkpoint(const char *dir, int32_t level, bmxg_particles *out, int64_t cap, int64_t *n);
+
+/* Message of the last failed fixture I/O call of this thread. */
+const char *bmxg_io_last_error(void);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* FP32F sphere steps keep a neighbour list with a skin between builds when it

@@ -23,6 +23,9 @@ Cases:
   init_bonds     InitBonds (bmx_pc_interaction.cpp:500-626 + fixBonds) on 400
                  rod segments with their bond tables cleared, a few tables
                  holding an unrelated bond first, and 100 spheres mixed in
+  fungi_network  the 410-segment hyphal network of the reference's checkpoint
+                 exec/fungi/chk357900 (level 2, read with bmxg_read_checkpoint),
+                 deck exec/fungi/input_fungi, 5 steps at the stable rod step
 """
 import math
 import os
@@ -271,10 +274,21 @@ def init_bonds():
     print(f"init_bonds: n={n} added={added} prior={len(pre)}")
 
 
+def fungi_network():
+    from boltzmannmfx_gb300.runtime import read_checkpoint
+    kv = deck(os.path.join(REF, "exec/fungi/input_fungi"))
+    prm = params_from_deck(kv)
+    geom = geom_from_deck(kv)
+    P = read_checkpoint(os.path.join(REF, "exec/fungi/chk357900/particles"), 2)
+    for k in ("velx", "vely", "velz", "wx", "wy", "wz"):
+        P[k][:] = 0.0
+    run_case("fungi_network", prm, geom, P, configs.ROD_DT, 5)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.have_ref():
         sys.exit("reference harness not built (reference tree missing?)")
     for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance,
-              init_bonds):
+              init_bonds, fungi_network):
         f()

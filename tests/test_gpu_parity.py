@@ -39,7 +39,8 @@ def readback(ctx, P):
     return Q
 
 
-@pytest.mark.parametrize("case", ["sphere_plain", "pair_test", "rods_small", "mixed", "half_bond", "wall_test"])
+@pytest.mark.parametrize("case", ["sphere_plain", "pair_test", "rods_small", "mixed", "half_bond", "wall_test",
+                                  "fungi_network"])
 def test_pairs_bitexact_golden(gpu_lib, case):
     d = load(case)
     ctx = gpu_ctx(params_of(d), [geom_of(d)], particles_of(d))
@@ -65,7 +66,7 @@ def test_sphere_fp64_bitexact_golden(gpu_lib, case):
         assert np.array_equal(Q[k], d["sN_" + k]), k
 
 
-@pytest.mark.parametrize("case", ["rods_small", "mixed", "half_bond", "wall_test"])
+@pytest.mark.parametrize("case", ["rods_small", "mixed", "half_bond", "wall_test", "fungi_network"])
 def test_rod_fp64_golden(gpu_lib, oracle_lib, case):
     """Within 1e-10 of the field's scale, plus the reference's own sensitivity
     to a one-ulp change of the segment angles (trig_floor): CUDA's and glibc's

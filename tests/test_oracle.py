@@ -11,7 +11,7 @@ from boltzmannmfx_gb300 import configs
 from boltzmannmfx_gb300.abi import FUNGI, YEAST, Geometry, Particles
 from common import geom_of, load, mirror, params_of, particles_of
 
-CASES = ["sphere_plain", "rods_small", "mixed", "half_bond", "pair_test", "wall_test"]
+CASES = ["sphere_plain", "rods_small", "mixed", "half_bond", "pair_test", "wall_test", "fungi_network"]
 CHECK = ("x", "y", "z", "theta", "phi", "velx", "vely", "velz", "wx", "wy", "wz",
          "n_bnds", "seg_id1", "seg_id2", "site", "position", "fix_site", "dltd",
          "fuse_flag", "split_flag", "new_flag")
