@@ -1043,6 +1043,47 @@ int bmxg_get_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int8_t *img, int6
     return BMXG_OK;
 }
 
+int bmxg_particle_exchange(bmxg_ctx *ctx, const double *vol, double *conc, double dt, const double *xpar,
+                           int32_t where)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (!vol || !conc || !xpar || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "vol, conc, xpar and a finite dt are required");
+    if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
+    const int64_t n = ctx->n;
+    if (n == 0 || !ctx->S.has_rods) return BMXG_OK;  // only FUNGI segments exchange
+    if (int rc0 = ensure_exact(ctx)) return rc0;
+    cudaStream_t st = ctx->stream;
+    const cudaMemcpyKind in = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    const cudaMemcpyKind back = (where == BMXG_HOST) ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    double *buf = nullptr;  // caller-order staging (3n), slot-order vol (n), conc (3n), out (3n)
+    CK(cudaMallocAsync((void **)&buf, sizeof(double) * 10 * n, st));
+    double *stage = buf, *svol = buf + 3 * n, *sc = buf + 4 * n, *so = buf + 7 * n;
+    const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, n);
+    cudaError_t e = cudaMemcpyAsync(stage, vol, sizeof(double) * n, in, st);
+    int launched = 0;
+    if (e == cudaSuccess) {
+        launched += launch_gather_d(svol, stage, ctx->S.orig, (int)n, grd, blk, st);
+        e = cudaMemcpyAsync(stage, conc, sizeof(double) * 3 * n, in, st);
+    }
+    if (e == cudaSuccess) {
+        for (int k = 0; k < 3; ++k)
+            launched += launch_gather_d(sc + (size_t)k * n, stage + (size_t)k * n, ctx->S.orig, (int)n, grd, blk, st);
+        launched += launch_exchange(ctx->S, dev_params(ctx->prm), ctx->parity, svol, sc, so, dt, xpar, grd, blk, st);
+        for (int k = 0; k < 3; ++k)
+            launched += launch_scatter_d(stage + (size_t)k * n, so + (size_t)k * n, ctx->S.orig, (int)n, grd, blk, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(conc, stage, sizeof(double) * 3 * n, back, st);
+    cudaFreeAsync(buf, st);
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    ctx->launches += launched;
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("particle exchange: ") + cudaGetErrorString(e));
+    return BMXG_OK;
+}
+
 int bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode)
 {
     if (!ctx) return BMXG_ERR_ARG;

@@ -150,6 +150,9 @@ int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int 
 int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
                       cudaStream_t st);
 int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st);
+// one ParticleExchange substep: conc / out 3 planes (A, B, C), slot order; xpar host
+int launch_exchange(const DevState &S, const DevParams &P, int a, const double *vol, const double *conc, double *out,
+                    double dt, const double *xpar, int grid, int block, cudaStream_t st);
 // start-up bond detection; counts[0] += bonds added, counts[1] += bonds past four
 int launch_init_bonds(const DevState &S, const DevParams &P, int a, double rlim, unsigned long long *counts,
                       int grid, int block, cudaStream_t st);

@@ -570,7 +570,78 @@ __global__ void k_init_bonds(const DevState S, const DevParams P, int a, double 
     }
 }
 
+// ---- ParticleExchange --------------------------------------------------------
+// One substep of BMXParticleContainer::ParticleExchange (bmx_pc_xchng.cpp:13-257)
+// with initExchange / evaluateExchange / applyIncrements
+// (bmx_chem_K.H:1949-2126): over the step's neighbour list, every FUNGI
+// segment i sums, for each listed FUNGI neighbour j that i and j both hold in
+// their bond tables, -d / vol_i with d = (c_i - c_j) * area * mt * dt
+// (area = pi (r_i^2 + r_j^2) / 2), d clamped so that neither side loses more
+// than its concentration over its bond count, and adds the sum to its
+// concentrations.  The reference's write to j's increment goes to a by-value
+// neighbour copy and is lost; the result reads only concentrations from
+// before the substep, so the kernel writes a separate output.  Same
+// arithmetic, in the same order, as the reference (FP64, no contraction).
+__global__ void k_exchange(const DevState S, const DevParams P, int a, const double *vol, const double *conc,
+                           double *out, double dt, double mtA, double mtB, double mtC)
+{
+    const int n = S.n;
+    const double pi = 3.14159265358979323846;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a1 = conc[i], b1 = conc[(size_t)n + i], c1 = conc[(size_t)2 * n + i];
+        double inc[3] = {0.0, 0.0, 0.0};
+        if (S.ctype[i] == kFungi) {
+            const DevGeom &G = geom_of(S, i);
+            int bx, by;
+            col_to_bxy(G, S.col[a][i], bx, by);
+            const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
+            int tb[13];
+            for (int k = 0; k < 13; ++k) tb[k] = S.tab[a][(size_t)k * n + i];
+            const int iid = S.id[i], icpu = S.cpu[i];
+            const double r1 = S.rad[i], v1 = vol[i];
+            const double area1 = pi * r1 * r1;
+            const double ni = (double)tb[0];
+            visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+                if (S.ctype[j] != kFungi) return;
+                if (!G.nbh_trivial) {  // BMXCheckPair: j is in i's list only within the neighbourhood
+                    double d[3];
+                    if (!(sep64(S, G, a, j, sx, sy, xi, yi, zi, d) <= P.nbh)) return;
+                }
+                if (find_in_table(tb, S.id[j], S.cpu[j]) < 0) return;
+                if (find_in_plane_table(S.tab[a], n, j, iid, icpu) < 0) return;
+                const double a2 = conc[j], b2 = conc[(size_t)n + j], c2 = conc[(size_t)2 * n + j];
+                const double r2 = S.rad[j], v2 = vol[j];
+                const double area2 = pi * r2 * r2;
+                const double area = 0.5 * (area1 + area2);
+                const double nj = (double)S.tab[a][j];
+                double dA = (a1 - a2) * area * mtA * dt;
+                double dB = (b1 - b2) * area * mtB * dt;
+                double dC = (c1 - c2) * area * mtC * dt;
+                if (dA / v1 > a1 / ni) dA = a1 * v1 / ni;
+                if (-dA / v2 > a2 / nj) dA = -a2 * v2 / nj;
+                if (dB / v1 > b1 / ni) dB = b1 * v1 / ni;
+                if (-dB / v2 > b2 / nj) dB = -b2 * v2 / nj;
+                if (dC / v1 > c1 / ni) dC = c1 * v1 / ni;
+                if (-dC / v2 > c2 / nj) dC = -c2 * v2 / nj;
+                inc[0] -= dA / v1;
+                inc[1] -= dB / v1;
+                inc[2] -= dC / v1;
+            });
+        }
+        out[i] = a1 + inc[0];
+        out[(size_t)n + i] = b1 + inc[1];
+        out[(size_t)2 * n + i] = c1 + inc[2];
+    }
+}
+
 }  // namespace
+
+int launch_exchange(const DevState &S, const DevParams &P, int a, const double *vol, const double *conc, double *out,
+                    double dt, const double *xpar, int grid, int block, cudaStream_t st)
+{
+    k_exchange<<<grid, block, 0, st>>>(S, P, a, vol, conc, out, dt, xpar[0], xpar[1], xpar[2]);
+    return 1;
+}
 
 int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st)
 {

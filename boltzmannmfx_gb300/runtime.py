@@ -25,7 +25,8 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_evolve_particles", "bmxg_evolve_particles_aos", "bmxg_get_stats",
                "bmxg_set_profiling", "bmxg_get_pairs", "bmxg_set_ext", "bmxg_forward",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
-               "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk", "bmxg_read_checkpoint",
+               "bmxg_particle_exchange", "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk",
+               "bmxg_read_checkpoint",
                "bmxg_io_last_error", "bmxg_autotune")
 
 
@@ -72,6 +73,8 @@ def load_library(path=None):
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.bmxg_set_list_mode.argtypes = [vp, C.c_int32]
+    dp = C.POINTER(C.c_double)
+    L.bmxg_particle_exchange.argtypes = [vp, dp, dp, C.c_double, dp, C.c_int32]
     PS = C.POINTER(ParticlesStruct)
     L.bmxg_read_ascii.argtypes = [C.c_char_p, PS, C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_write_ascii.argtypes = [C.c_char_p, PS]
@@ -182,6 +185,17 @@ class Context:
                                             idx.ctypes.data_as(C.POINTER(C.c_int32)),
                                             img.ctypes.data_as(C.POINTER(C.c_int8)), cap, C.byref(total)))
         return offs, idx[:total.value], img[:total.value]
+
+    def particle_exchange(self, vol, conc, dt, xpar):
+        """One ParticleExchange substep on the loaded state: returns the new
+        concentrations (3, n) of species A, B, C (caller order)."""
+        c = np.ascontiguousarray(conc, np.float64).reshape(-1).copy()
+        v = np.ascontiguousarray(vol, np.float64)
+        x = np.ascontiguousarray(xpar, np.float64)
+        dp = C.POINTER(C.c_double)
+        self._check(self.lib.bmxg_particle_exchange(self.h, v.ctypes.data_as(dp), c.ctypes.data_as(dp), dt,
+                                                    x.ctypes.data_as(dp), abi.BMXG_HOST))
+        return c.reshape(3, self.n)
 
     def set_list_mode(self, mode):
         """1: FP32F sphere steps use the skin neighbour list where it is exact; 0: never."""

@@ -300,6 +300,23 @@ int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *ge
  * here they are dropped and the call returns BMXG_ERR_CAPACITY. */
 int  bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow);
 
+/* ---- species exchange between bonded segments ---------------------------- */
+
+/* One substep of BMXParticleContainer::ParticleExchange
+ * (src/des/bmx_pc_xchng.cpp:13-257, with initExchange / evaluateExchange /
+ * applyIncrements of src/chemistry/bmx_chem_K.H:1949-2126) on the CURRENT
+ * state and its neighbour list: each FUNGI segment exchanges species A, B, C
+ * with every listed FUNGI neighbour that both hold in their bond tables,
+ * d = (c_i - c_j) * pi (r_i^2 + r_j^2) / 2 * mt * dt, clamped as the
+ * reference clamps it, and adds -d / vol_i.  conc: 3 planes of n (A, B, C;
+ * caller order), updated in place; vol: n; xpar = {mass_transfer_A, _B, _C}
+ * (BMXChemistry::getExchangeParameters, src/chemistry/bmx_chem.cpp:221-228).
+ * where: BMXG_HOST or BMXG_DEVICE for conc and vol (xpar is a host array).  The reference keeps the
+ * concentrations in the particles' real data (realIdx::first_data + 0..2);
+ * here they are the caller's arrays. */
+int  bmxg_particle_exchange(bmxg_ctx *ctx, const double *vol, double *conc, double dt,
+                            const double xpar[3], int32_t where);
+
 /* ---- fixture I/O (host only; no context, no device) ---------------------- */
 
 /* Particle input file of BMXParticleContainer::InitParticlesAscii

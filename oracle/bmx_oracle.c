@@ -913,3 +913,65 @@ int orc_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_parti
     if (overflow) *overflow = nover;
     return BMXG_OK;
 }
+
+/* ParticleExchange (bmx_pc_xchng.cpp:13-257; initExchange, evaluateExchange,
+ * applyIncrements of bmx_chem_K.H:1949-2126), one substep over the given
+ * neighbour list.  conc: 3 planes (A, B, C) of n, updated in place; vol: n.
+ * For each FUNGI segment i: its increments start at zero; every listed
+ * FUNGI neighbour j that i and j both list as bonded moves
+ * d = (c_i - c_j) * area * mt * dt, area the mean septum cross-section
+ * pi (r_i^2 + r_j^2) / 2, clamped so that neither side can go negative in
+ * one bond's share (c / n_bnds), and i's increment changes by -d / vol_i
+ * (the write to j's increment lands on the by-value neighbour copy and is
+ * lost, as in the reference).  Then every segment adds its increments. */
+int orc_particle_exchange(const bmxg_geometry *geom, const bmxg_particles *p, const int64_t *offs,
+                          const int32_t *idx, const double *vol, double *conc, double dt,
+                          const double xpar[3])
+{
+    (void)geom;
+    if (!p || !offs || !vol || !conc || !xpar || p->n < 0) return BMXG_ERR_ARG;
+    if (!has_rod_fields(p)) return BMXG_ERR_ARG;
+    const int64_t N = p->n;
+    double *inc = (double *)calloc((size_t)(3 * N + 1), sizeof(double));
+    if (!inc) return BMXG_ERR_OOM;
+    const double pi = 3.14159265358979323846;
+    for (int64_t i = 0; i < N; ++i) {
+        if (p->cell_type[i] != BMXG_FUNGI) continue;
+        double *ci = inc + 3 * i;  /* initExchange */
+        ci[0] = ci[1] = ci[2] = 0.0;
+        for (int64_t t = offs[i]; t < offs[i + 1]; ++t) {
+            const int64_t j = idx[t];
+            if (p->cell_type[j] != BMXG_FUNGI) continue;
+            const int ib = find_bond(p, i, p->id[j], p->cpu[j]);
+            const int jb = find_bond(p, j, p->id[i], p->cpu[i]);
+            if (ib < 0 || jb < 0) continue;
+            const double a1 = conc[i], b1 = conc[N + i], c1 = conc[2 * N + i];
+            const double a2 = conc[j], b2 = conc[N + j], c2 = conc[2 * N + j];
+            const double r1 = p->radius[i], r2 = p->radius[j];
+            const double area1 = pi * r1 * r1, area2 = pi * r2 * r2;
+            const double v1 = vol[i], v2 = vol[j];
+            const double area = 0.5 * (area1 + area2);
+            double dA = (a1 - a2) * area * xpar[0] * dt;
+            double dB = (b1 - b2) * area * xpar[1] * dt;
+            double dC = (c1 - c2) * area * xpar[2] * dt;
+            const double ni = (double)p->n_bnds[i], nj = (double)p->n_bnds[j];
+            if (dA / v1 > a1 / ni) dA = a1 * v1 / ni;
+            if (-dA / v2 > a2 / nj) dA = -a2 * v2 / nj;
+            if (dB / v1 > b1 / ni) dB = b1 * v1 / ni;
+            if (-dB / v2 > b2 / nj) dB = -b2 * v2 / nj;
+            if (dC / v1 > c1 / ni) dC = c1 * v1 / ni;
+            if (-dC / v2 > c2 / nj) dC = -c2 * v2 / nj;
+            ci[0] -= dA / v1;
+            ci[1] -= dB / v1;
+            ci[2] -= dC / v1;
+        }
+    }
+    for (int64_t i = 0; i < N; ++i) {  /* applyIncrements */
+        if (p->cell_type[i] != BMXG_FUNGI) continue;
+        conc[i] += inc[3 * i];
+        conc[N + i] += inc[3 * i + 1];
+        conc[2 * N + i] += inc[3 * i + 2];
+    }
+    free(inc);
+    return BMXG_OK;
+}

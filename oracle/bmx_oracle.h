@@ -66,6 +66,13 @@ int  orc_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_part
                     const int64_t *offs, const int32_t *idx, const int8_t *img, double rlim,
                     int64_t *added, int64_t *overflow);
 
+/* ParticleExchange over the given neighbour list (bmx_pc_xchng.cpp:13-257,
+ * bmx_chem_K.H:1949-2126): conc 3 planes (A, B, C) updated in place, vol per
+ * particle, xpar = {mass_transfer_A, _B, _C}. */
+int  orc_particle_exchange(const bmxg_geometry *geom, const bmxg_particles *p, const int64_t *offs,
+                           const int32_t *idx, const double *vol, double *conc, double dt,
+                           const double xpar[3]);
+
 /* Single-pair / single-particle entry points used by unit tests. */
 void orc_pair_force(const bmxg_params *prm, const double r12[3],
                     const bmxg_particles *p, int64_t i, int64_t j,

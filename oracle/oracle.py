@@ -62,6 +62,7 @@ def lib():
         L.orc_min_distance.argtypes = [_d, _d, _d]
         L.orc_min_distance.restype = None
         L.orc_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double, _i64, _i64]
+        L.orc_particle_exchange.argtypes = [_G, _S, _i64, _i32, _d, _d, C.c_double, _d]
         _lib = L
     return _lib
 
@@ -88,6 +89,7 @@ def reflib():
         L.ref_surface_force.argtypes = [_P, _S, C.c_int64, _d, _d]
         L.ref_surface_force.restype = None
         L.ref_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double]
+        L.ref_particle_exchange.argtypes = [_S, _i64, _i32, _i8, _G, _d, _d, C.c_double, _d]
         _ref = L
     return _ref
 
@@ -246,3 +248,44 @@ def init_bonds(params, geom, P, pl=None, rlim=RLIM, use_ref=False):
     if rc != BMXG_OK:
         raise RuntimeError(f"orc_init_bonds failed: {rc}")
     return added.value, over.value
+
+
+def _quiet(call):
+    """Run call() with the process's stdout sent to /dev/null (the
+    reference's loop bodies print per particle)."""
+    libc = C.CDLL(None)
+    libc.fflush(None)
+    saved = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(null, 1)
+    try:
+        rc = call()
+        libc.fflush(None)
+    finally:
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(null)
+    return rc
+
+
+def particle_exchange(geom, P, vol, conc, dt, xpar, pl=None, params=None, use_ref=False):
+    """One ParticleExchange substep; returns the new concentrations (3, n)."""
+    if pl is None:
+        pl = pairs(params, geom, P)
+    offs, idx, img = pl
+    idx = np.ascontiguousarray(idx if len(idx) else np.zeros(1, np.int32), np.int32)
+    img = np.ascontiguousarray(img if len(img) else np.zeros(1, np.int8), np.int8)
+    c = np.ascontiguousarray(conc, np.float64).reshape(-1).copy()
+    v = np.ascontiguousarray(vol, np.float64)
+    xp = np.ascontiguousarray(xpar, np.float64)
+    s = P.struct()
+    if use_ref:
+        rc = _quiet(lambda: reflib().ref_particle_exchange(C.byref(s), offs.ctypes.data_as(_i64),
+                                                           idx.ctypes.data_as(_i32), img.ctypes.data_as(_i8),
+                                                           C.byref(geom), _dp(v), _dp(c), dt, _dp(xp)))
+    else:
+        rc = lib().orc_particle_exchange(C.byref(geom), C.byref(s), offs.ctypes.data_as(_i64),
+                                         idx.ctypes.data_as(_i32), _dp(v), _dp(c), dt, _dp(xp))
+    if rc != BMXG_OK:
+        raise RuntimeError(f"particle exchange failed: {rc}")
+    return c.reshape(3, P.n)

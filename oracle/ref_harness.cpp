@@ -10,6 +10,9 @@
 //   * the body of the force-gather lambda, src/des/bmx_pc_interaction.cpp:174-278
 //   * the body of the update lambda,       src/des/bmx_pc_interaction.cpp:317-436
 //   * the body of the InitBonds lambda,    src/des/bmx_pc_interaction.cpp:577-626
+//   * the body of the exchange lambda,     src/des/bmx_pc_xchng.cpp:122-151, with
+//     initExchange / evaluateExchange / applyIncrements of
+//     src/chemistry/bmx_chem_K.H (included verbatim)
 //     (cut out of the reference file by oracle/Makefile into _ref/ and
 //     #included below inside plain loops over i, i.e. the serial CPU build).
 // What is NOT the reference's code: the neighbour list and the periodic wrap
@@ -22,6 +25,7 @@
 #include <vector>
 
 #include <bmx_cell_interaction_K.H>
+#include <bmx_chem_K.H>
 
 #include "bmx_oracle.h"
 
@@ -255,6 +259,55 @@ int ref_init_bonds(const bmxg_params *prm, const bmxg_geometry *geom, bmxg_parti
     }
     (void)small_number;
     from_aos(parts, p);
+    return BMXG_OK;
+}
+
+// ParticleExchange with the reference's loop body (bmx_pc_xchng.cpp:122-151)
+// and applyIncrements, serial over i.  conc: 3 planes (A, B, C) of n, in and
+// out; vol: n.  The concentrations live in the chemistry block of the real
+// data (realIdx::first_data + 0..2, increments at + 3..5).
+int ref_particle_exchange(const bmxg_particles *p, const int64_t *offs, const int32_t *idx, const int8_t *img,
+                          const bmxg_geometry *geom, const double *vol, double *conc, double dt, const double *xp)
+{
+    if (!p || !offs || !vol || !conc || !xp || !geom) return BMXG_ERR_ARG;
+    std::vector<RefParticle> parts;
+    to_aos(p, parts);
+    const int64_t n = p->n;
+    for (int64_t i = 0; i < n; ++i) {
+        RefParticle &q = parts[(size_t)i];
+        q.m_rdata[realIdx::vol] = vol[i];
+        for (int k = 0; k < 3; ++k) q.m_rdata[realIdx::first_data + k] = conc[(size_t)k * n + i];
+    }
+    const std::vector<RefParticle> ghosts = parts;  // neighbours as copies taken when the loop starts
+    const double lx = geom->prob_hi[0] - geom->prob_lo[0];
+    const double ly = geom->prob_hi[1] - geom->prob_lo[1];
+    struct {
+        const RefParticle *g;
+        const int64_t *o;
+        const int32_t *ix;
+        const int8_t *im;
+        double lx, ly;
+        NbrRange getNeighbors(int i) const
+        {
+            return NbrRange{NbrIter{g, ix, im, o[i], lx, ly}, NbrIter{g, ix, im, o[i + 1], lx, ly}};
+        }
+    } nbor_data{ghosts.data(), offs, idx, img, lx, ly};
+    std::vector<Real> xpar_vec(xp, xp + 3);
+    Real *xpar = &xpar_vec[0];
+    const int nrp = (int)n, ntot = nrp;
+    RefParticle *pstruct = parts.data();
+    const Real subdt = dt;
+    // stdout of the body's diagnostics goes where the caller sends it
+    for (int i = 0; i < nrp; ++i) {
+#include "xchng_body.inc"
+    }
+    (void)ntot;
+    for (int i = 0; i < nrp; ++i) {
+        auto &particle = pstruct[i];
+        applyIncrements(&particle.rdata(0), &particle.idata(0));
+    }
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) conc[(size_t)k * n + i] = parts[(size_t)i].m_rdata[realIdx::first_data + k];
     return BMXG_OK;
 }
 

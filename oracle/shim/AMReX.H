@@ -1,5 +1,5 @@
 // Minimal stand-in for the AMReX umbrella header, enough for the reference's
-// header-only force kernels (src/chemistry/bmx_cell_interaction_K.H) to compile
+// header-only kernels (src/chemistry/bmx_cell_interaction_K.H, bmx_chem_K.H) to compile
 // as plain host C++. Oracle infrastructure only; never part of the product.
 #ifndef BMXG_SHIM_AMREX_H
 #define BMXG_SHIM_AMREX_H
@@ -12,8 +12,15 @@
 #define AMREX_GPU_HOST
 #define AMREX_INLINE inline
 #define AMREX_FORCE_INLINE inline
+#include <cstdlib>
+#include <iostream>  // the chemistry kernels print with std::cout
 namespace amrex {
 using Real = double;
 template <class T> using Vector = std::vector<T>;
+// bmx_chem_K.H's segment-splitting and fusion kernels take a random engine;
+// the exchange kernels the oracle uses do not call it
+struct RandomEngine {};
+inline Real Random(RandomEngine const &) { return 0.5; }
+inline void Abort(const char *msg) { std::fprintf(stderr, "%s\n", msg); std::abort(); }
 }
 #endif

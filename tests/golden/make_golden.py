@@ -23,6 +23,9 @@ Cases:
   init_bonds     InitBonds (bmx_pc_interaction.cpp:500-626 + fixBonds) on 400
                  rod segments with their bond tables cleared, a few tables
                  holding an unrelated bond first, and 100 spheres mixed in
+  exchange       ParticleExchange (bmx_pc_xchng.cpp:122-151 + bmx_chem_K.H) on the
+                 network below with seeded concentrations, a gentle and a
+                 clamping mass-transfer rate
   fungi_network  the 410-segment hyphal network of the reference's checkpoint
                  exec/fungi/chk357900 (level 2, read with bmxg_read_checkpoint),
                  deck exec/fungi/input_fungi, 5 steps at the stable rod step
@@ -285,10 +288,32 @@ def fungi_network():
     run_case("fungi_network", prm, geom, P, configs.ROD_DT, 5)
 
 
+def exchange():
+    d = dict(np.load(os.path.join(OUT, "fungi_network.npz")))
+    prm = Params()
+    for (k, _), v in zip(Params._fields_, d["params"]):
+        setattr(prm, k, float(v))
+    geom = Geometry.make(d["lo"], d["hi"], d["n_cell"], d["periodic"])
+    P = Particles(len(d["in_x"]), rods=True)
+    for k in P.a:
+        if "in_" + k in d:
+            P.a[k][...] = d["in_" + k]
+    rng = np.random.default_rng(29)
+    conc = rng.uniform(0.0, 1.0e-3, (3, P.n))
+    vol = math.pi * P["radius"] ** 2 * P["c_length"]
+    pl = O.pairs(prm, geom, P)
+    out = {"conc": conc, "vol": vol, "dt": np.array(0.25)}
+    for name, xp in (("gentle", [1.0e-2, 2.0e-2, 5.0e-3]), ("clamped", [1.0e4, 1.0e4, 1.0e4])):
+        out["xpar_" + name] = np.array(xp)
+        out["out_" + name] = O.particle_exchange(geom, P, vol, conc, 0.25, xp, pl=pl, use_ref=True)
+    np.savez_compressed(os.path.join(OUT, "exchange.npz"), **out)
+    print("exchange:", P.n)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.have_ref():
         sys.exit("reference harness not built (reference tree missing?)")
     for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance,
-              init_bonds, fungi_network):
+              init_bonds, fungi_network, exchange):
         f()
