@@ -388,27 +388,38 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
             if (off[c + 1] < off[c]) return fail(ctx, BMXG_ERR_ARG, "colony_offsets must not decrease");
     }
     const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    // cell types decide which path runs; rods need their fields
-    std::vector<int32_t> ct((size_t)n);
-    if (n) {
-        if (where == BMXG_HOST) std::memcpy(ct.data(), p->cell_type, sizeof(int32_t) * n);
-        else CK(cudaMemcpy(ct.data(), p->cell_type, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-    }
+    // cell types decide which path runs (rods need their fields) and the
+    // largest radius whether the FP32F list is exact: checked on the device
+    // (the arrays go there anyway), one small read-back
     bool rods = false;
-    for (int64_t i = 0; i < n; ++i) {
-        if (ct[i] != BMXG_YEAST && ct[i] != BMXG_FUNGI) return fail(ctx, BMXG_ERR_ARG, "cell_type must be 0 or 1");
-        rods |= (ct[i] == BMXG_FUNGI);
-    }
-    double rmax = 0.0;  // decides whether the FP32F list is exact for this state
-    {
-        std::vector<double> rr;
-        const double *r = p->radius;
-        if (where == BMXG_DEVICE && n) {
-            rr.resize((size_t)n);
-            CK(cudaMemcpy(rr.data(), p->radius, sizeof(double) * n, cudaMemcpyDeviceToHost));
-            r = rr.data();
+    double rmax = 0.0;
+    if (n) {
+        cudaStream_t st0 = ctx->stream;
+        unsigned long long *chk = nullptr;
+        int *dct = nullptr;
+        double *dr = nullptr;
+        unsigned long long h[4] = {0, 0, 0, 0};
+        CK(cudaMallocAsync((void **)&chk, sizeof(h) + sizeof(int) * n + sizeof(double) * n + 64, st0));
+        dr = (double *)((char *)chk + 64);
+        dct = (int *)(dr + n);
+        cudaError_t e = cudaMemsetAsync(chk, 0, sizeof(h), st0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dct, p->cell_type, sizeof(int) * n, kind, st0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dr, p->radius, sizeof(double) * n, kind, st0);
+        if (e == cudaSuccess) {
+            Shape sh;
+            launch_check_state(dct, dr, (int)n, chk, grid_for(ctx, sh, n), sh.block, st0);
+            e = cudaGetLastError();
         }
-        for (int64_t i = 0; i < n; ++i) rmax = (r[i] > rmax || r[i] != r[i]) ? r[i] : rmax;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, chk, sizeof(h), cudaMemcpyDeviceToHost, st0);
+        cudaFreeAsync(chk, st0);
+        const cudaError_t e2 = cudaStreamSynchronize(st0);
+        if (e == cudaSuccess) e = e2;
+        if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("state check: ") + cudaGetErrorString(e));
+        if (h[0]) return fail(ctx, BMXG_ERR_ARG, "cell_type must be 0 or 1");
+        rods = h[1] != 0;
+        const uint64_t rb = h[2];
+        std::memcpy(&rmax, &rb, sizeof(rmax));
+        if (h[3]) rmax = std::nan("");
     }
     if (rods && (!p->c_length || !p->theta || !p->phi || !p->area || !p->id || !p->cpu || !p->n_bnds ||
                  !p->seg_id1 || !p->seg_id2 || !p->site))
@@ -543,10 +554,11 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         if ((rc = up_i(p->site, S.tab[0] + 9 * n, 4, 0))) return rc;
         LAUNCH(launch_trig(S, 0, grd, blk, st));
     }
-    // bins of the slots and the first column lists
+    // bins of the slots and the first column lists: the sort above already
+    // has them (slot s is sorted position s)
     CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
-    LAUNCH(launch_bin(S, 0, grd, blk, st));
-    LAUNCH(launch_rebuild(S, 0, ctx->scan_scratch, grd, blk, st));
+    CK(cudaMemcpyAsync(S.colstart[0], S.colstart[1], sizeof(int) * (ncols + 1), cudaMemcpyDeviceToDevice, st));
+    LAUNCH(launch_slot_init(S, S.col[1], S.iz[1], ctx->uperm, grd, blk, st));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->have_state = true;
@@ -579,25 +591,24 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     const int blk = ctx->sh_misc.block;
     const int grd = grid_for(ctx, ctx->sh_misc, n);
     const int a = ctx->parity;
+    // one staging buffer per kind: the stream orders each copy before the
+    // next scatter into it; one synchronisation at the end
     auto out_d = [&](double *dst, const double *src) -> int {
         if (!dst || !src) return BMXG_OK;
         LAUNCH(launch_scatter_d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
         CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
-        CK(cudaStreamSynchronize(st));
         return BMXG_OK;
     };
     auto out_i = [&](int32_t *dst, const int *src, int planes) -> int {
         if (!dst || !src) return BMXG_OK;
         LAUNCH(launch_scatter_i(ctx->ui, src, S.orig, (int)n, planes, grd, blk, st));
         CK(cudaMemcpyAsync(dst, ctx->ui, sizeof(int) * n * planes, kind, st));
-        CK(cudaStreamSynchronize(st));
         return BMXG_OK;
     };
     auto out_f = [&](double *dst, const float *src) -> int {  // FP32F velocities, widened
         if (!dst || !src) return BMXG_OK;
         LAUNCH(launch_scatter_f2d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
         CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
-        CK(cudaStreamSynchronize(st));
         return BMXG_OK;
     };
     int rc;
@@ -636,8 +647,8 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     } else if (ctx->stepped) {
         for (int32_t *f : {p->fuse_flag, p->split_flag, p->new_flag})
             if (f) CK(cudaMemsetAsync(f, 0, sizeof(int32_t) * n, st));
-        CK(cudaStreamSynchronize(st));
     }
+    CK(cudaStreamSynchronize(st));
     return BMXG_OK;
 }
 
@@ -667,6 +678,7 @@ void prof_events(bmxg_ctx *ctx, cudaEvent_t *k0, cudaEvent_t *k1)
 // ---- FP32F neighbour list with a skin ---------------------------------------
 constexpr int kListMaxAge = 64;      // bounds the FP32 drift of the frozen-frame offsets
 constexpr int kListExactEvery = 8;   // builds between exact FP64 re-binnings
+constexpr int kListMinSteps = 2;     // shorter calls on a state without a list run the per-step path
 
 // Skin of the list for the loaded state and parameters, or 0 where the list
 // would not reproduce the reference's pair set: the largest cutoff
@@ -719,7 +731,9 @@ int ensure_list(bmxg_ctx *ctx, float skin)
         h.inc_max[k] = 0x007fffffu;
     }
     h.max_age = kListMaxAge;
-    h.force = 1;
+    // a state whose list bins (buffer kListBins) are the exact bins of its
+    // current positions needs no FP64 re-binning for the first build
+    h.force = (ctx->bins_exact && ctx->parity == kListBins) ? 2 : 1;
     h.exact_every = kListExactEvery;
     CK(cudaMemcpyAsync(S.lctl, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -876,8 +890,12 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     // nsubsteps = ceil(dt / dtsolid) with dtsolid := dt, subdt = dt / nsubsteps
     // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
     const double subdt = dt / 1.0;
-    // FP32F spheres use the neighbour list wherever it reproduces the pair set
-    const float skin = (precision == BMXG_FP32F && ctx->list_mode) ? list_skin(ctx) : 0.0f;
+    // FP32F spheres use the neighbour list wherever it reproduces the pair set,
+    // and where the calls are long enough to amortise a build: a call of
+    // fewer than kListMinSteps steps on a state without a valid list takes
+    // the per-step path
+    float skin = (precision == BMXG_FP32F && ctx->list_mode) ? list_skin(ctx) : 0.0f;
+    if (skin > 0.0f && !ctx->list_valid && nsteps < kListMinSteps) skin = 0.0f;
     if (skin > 0.0f) {
         int rc = ensure_list(ctx, skin);
         if (rc) return rc;

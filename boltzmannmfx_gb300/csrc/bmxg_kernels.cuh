@@ -23,7 +23,8 @@ struct ListCtl {
     float eps_step;        // FP32 rounding of one position update, added per step
     int age;               // steps since the last build
     int max_age;           // rebuild at least this often (bounds FP32 offset drift)
-    int force;             // nonzero: rebuild at the next step (state changed)
+    int force;             // rebuild at the next step: 1 state changed, 2 state changed but the
+                           // list bins hold its exact bins (no FP64 re-binning needed)
     int rebuild;           // this step's decision (read by the gated kernels)
     int exact_every;       // every exact_every-th build re-bins from the FP64 positions
     int exact_now;         // this build does (the others move frames in FP32)
@@ -104,6 +105,13 @@ int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStre
                          const int *gate = nullptr);
 int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st,
                    int ra = -1, const int *gate = nullptr);
+
+// bins, offsets and identity column order of a freshly sorted state (buffer 0)
+int launch_slot_init(const DevState &S, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
+                     cudaStream_t st);
+// state checks before a load: out[4] = {bad cell type, any FUNGI, largest radius bits, NaN radius}
+int launch_check_state(const int *ct, const double *r, int n, unsigned long long *out, int grid, int block,
+                       cudaStream_t st);
 
 // caller-order staging -> slot order (set_state) and back (get_state)
 int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz,

@@ -120,13 +120,11 @@ __device__ __forceinline__ void col_to_bxy(const DevGeom &G, int col, int &bx, i
 // Bin a slot at position (x, y, z): column and z bin into buffer bb, FP32
 // offsets from the bin corner into buffer rb, column count; flag
 // out-of-domain z, images that leave their halo cell, and non-finite positions.
-__device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom &G, int i, double x, double y,
-                                                double z, double r, int bb, int rb, bool count_domain = true,
-                                                bool count_col = true)
+// place_slot does the same for bins already known.
+__device__ __forceinline__ void place_slot(const DevState &S, const DevGeom &G, int i, double x, double y,
+                                           double z, double r, int bb, int rb, int bx, int by, int bz,
+                                           bool count_domain, bool count_col)
 {
-    const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
-    const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
-    const int bz = bin_of(z, G.plo[2], G.dxi[2], 1, G.n[2]);
     const int c = column_of(G, bx, by);
     S.col[bb][i] = c;
     S.iz[bb][i] = bz;
@@ -147,6 +145,16 @@ __device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom
         const int gb = bin_of(y + (double)sy * G.len[1], G.plo[1], G.dxi[1], 0, G.n[1] + 1);
         if (gb != (sy > 0 ? G.n[1] + 1 : 0)) atomicAdd(&S.cnt->edge_ghost, 1ULL);
     }
+}
+
+__device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom &G, int i, double x, double y,
+                                                double z, double r, int bb, int rb, bool count_domain = true,
+                                                bool count_col = true)
+{
+    const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
+    const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
+    const int bz = bin_of(z, G.plo[2], G.dxi[2], 1, G.n[2]);
+    place_slot(S, G, i, x, y, z, r, bb, rb, bx, by, bz, count_domain, count_col);
 }
 
 // Bin a slot into buffer b (bins and offsets).

@@ -174,7 +174,9 @@ __global__ void k_user_scatter(const DevState S, const int *ucol, const int *col
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
         const int c = ucol[u];
         const int r = atomicSub(&S.colcnt[c], 1) - 1;
-        S.tmp[colstart[c] + r] = u;
+        const int t = colstart[c] + r;
+        if (t >= 0 && t < S.n) S.tmp[t] = u;
+        else atomicAdd(&S.cnt->bad_index, 1ULL);
     }
 }
 
@@ -183,14 +185,15 @@ __global__ void k_user_canon(const DevState S, const int *ucol, const int *uiz, 
 {
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
         const int c = ucol[u];
-        const int s0 = colstart[c], s1 = colstart[c + 1];
+        const int s0 = max(colstart[c], 0), s1 = min(colstart[c + 1], S.n);
         const unsigned long long key = col_key(uiz[u], u);
         int rank = 0;
         for (int t = s0; t < s1; ++t) {
             const int v = S.tmp[t];
-            rank += (col_key(uiz[v], v) < key);
+            if ((unsigned)v < (unsigned)S.n) rank += (col_key(uiz[v], v) < key);
         }
-        uperm[s0 + rank] = u;
+        if (s0 + rank < s1) uperm[s0 + rank] = u;
+        else atomicAdd(&S.cnt->bad_index, 1ULL);
     }
 }
 
@@ -273,7 +276,72 @@ __global__ void k_pairs(const DevState S, const DevParams P, int a, int64_t *cnt
     }
 }
 
+// Checks of a caller's state before it is loaded: cell types outside
+// {YEAST, FUNGI}, whether any FUNGI segment is present, the largest radius
+// (non-negative doubles order as their bit patterns) and whether any radius
+// is NaN.  out: {bad, fungi, rmax bits, nan}, zeroed by the caller.
+__global__ void k_check_state(const int *__restrict__ ct, const double *__restrict__ r, int n,
+                              unsigned long long *out)
+{
+    unsigned bad = 0, fungi = 0, nan = 0;
+    unsigned long long rmax = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned c = (unsigned)ct[i];
+        bad |= (c > 1u) ? 1u : 0u;
+        fungi |= (c == 1u) ? 1u : 0u;
+        const double v = r[i];
+        nan |= (v != v) ? 1u : 0u;
+        if (v > 0.0) rmax = max(rmax, (unsigned long long)__double_as_longlong(v));
+    }
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    fungi = __reduce_or_sync(0xffffffffu, fungi);
+    nan = __reduce_or_sync(0xffffffffu, nan);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicOr(&out[0], 1ull);
+        if (fungi) atomicOr(&out[1], 1ull);
+        if (rmax) atomicMax(&out[2], rmax);
+        if (nan) atomicOr(&out[3], 1ull);
+    }
+}
+
+// Slot s of a freshly sorted state holds caller particle uperm[s]: its bins
+// are the caller-order bins, its column order is the sort's (perm = identity,
+// colstart = the sort's offsets, copied by the caller); offsets and counters
+// as rebin_slot computes them, without computing the bins again.
+__global__ void k_slot_init(const DevState S, const int *ucol, const int *uiz, const int *uperm)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S.n; s += gridDim.x * blockDim.x) {
+        const DevGeom &G = geom_of(S, s);
+        const int u = uperm[s];
+        int bx, by;
+        col_to_bxy(G, ucol[u], bx, by);
+        place_slot(S, G, s, S.x[0][s], S.y[0][s], S.z[0][s], S.rad[s], 0, 0, bx, by, uiz[u], true, false);
+        S.perm[0][s] = s;
+        if (S.srel[0]) {
+            S.srel[0][s] = S.rel[0][s];
+            S.siz[0][s] = uiz[u];
+            S.rank[0][s] = s;
+        }
+    }
+}
+
 }  // namespace
+
+int launch_slot_init(const DevState &S, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
+                     cudaStream_t st)
+{
+    k_slot_init<<<grid, block, 0, st>>>(S, ucol, uiz, uperm);
+    return 1;
+}
+
+int launch_check_state(const int *ct, const double *r, int n, unsigned long long *out, int grid, int block,
+                       cudaStream_t st)
+{
+    k_check_state<<<grid, block, 0, st>>>(ct, r, n, out);
+    return 1;
+}
 
 int launch_bin(const DevState &S, int b, int grid, int block, cudaStream_t st)
 {

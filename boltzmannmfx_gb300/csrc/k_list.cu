@@ -84,7 +84,9 @@ __global__ void k_list_decide(ListCtl *c, cudaGraphConditionalHandle h, int use_
     const int age = c->age + 1;
     const bool rb = c->force != 0 || !(acc <= c->skin) || age > c->max_age;
     if (rb) {
-        c->exact_now = (c->force != 0 || c->builds % c->exact_every == 0) ? 1 : 0;
+        // force 1: state changed, bins unknown (exact); force 2: the list bins
+        // are already the exact bins of the positions (no FP64 re-binning)
+        c->exact_now = (c->force == 1 || (c->force == 0 && c->builds % c->exact_every == 0)) ? 1 : 0;
         for (int k = 0; k < 3; ++k) c->range[k] = 0.0f;
         c->acc = 0.0f;
         c->age = 0;
