@@ -708,8 +708,8 @@ int ensure_list(bmxg_ctx *ctx, float skin)
     DevState &S = ctx->S;
     if (!S.nbr) {
         int rc;
-        if ((rc = dalloc(ctx, &S.nbr, (size_t)kNbrCap * ctx->n))) return rc;
-        if ((rc = dalloc(ctx, &S.lmeta, ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.nbr, (size_t)(kNbrCap - kNbrInline) * ctx->n))) return rc;
+        if ((rc = dalloc(ctx, &S.lrec, ctx->n))) return rc;
         if ((rc = dalloc(ctx, &S.cellcnt, ctx->ncells_total))) return rc;
         if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
         if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints((int)ctx->ncells_total)))) return rc;

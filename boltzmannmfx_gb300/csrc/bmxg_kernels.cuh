@@ -34,6 +34,7 @@ struct ListCtl {
 };
 
 constexpr int kNbrCap = 32;          // list entries per slot (more: the slot walks its stencil)
+constexpr int kNbrInline = 3;        // entries held in the slot's list record beside its metadata
 constexpr int kNbrShift = 26;        // entry = slot | (shift code << 26)
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
 
@@ -80,8 +81,10 @@ struct DevState {
     double *fc;        // 6 planes, force gather of the rod path
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
-    int *nbr;          // kNbrCap planes of n entries: neighbour slot | (dx, dy, dz bin shift + 1) << 26
-    int *lmeta;        // per slot: z bin (bits 0-15), edge flags (16-18), list length (20-27, saturating)
+    int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry:
+                       // neighbour slot | (dx, dy, dz bin shift + 1) << 26
+    int4 *lrec;        // per slot: x = z bin (bits 0-15), edge flags (16-18), list length
+                       // (20-27, saturating); y, z, w = the first kNbrInline entries
     int *cellcnt;      // per 3D cell counter, zero between uses
     int *cellstart;    // ncells_total + 1 offsets of the cells in the sorted copies
     int ncells_total;

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
         const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
         const float lim0 = reach + 4.0e-6f * fmaxf(dxb, fmaxf(dyb, dzb));
         int c = 0;
+        int4 rec = make_int4(0, 0, 0, 0);
         visit_cells(S, G, t, bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
             const float4 q = __ldg(&S.srel[B][u]);
             const float ex = (me.x - q.x) - (float)dxs * dxb;
@@ -274,12 +275,17 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
             const float lim = (me.w + q.w) + lim0;
             if (!(r2f <= lim * lim)) return;
             const unsigned code = (unsigned)(dxs + 1) | ((unsigned)(dys + 1) << 2) | ((unsigned)(dzs + 1) << 4);
-            if (c < kNbrCap) S.nbr[(size_t)c * n + i] = (int)((unsigned)__ldg(&S.perm[B][u]) | (code << kNbrShift));
+            const int e = (int)((unsigned)__ldg(&S.perm[B][u]) | (code << kNbrShift));
+            if (c == 0) rec.y = e;
+            else if (c == 1) rec.z = e;
+            else if (c == 2) rec.w = e;
+            else if (c < kNbrCap) S.nbr[(size_t)(c - kNbrInline) * n + i] = e;
             ++c;
         });
         const int edge = ((G.per[0] && (bx == 1 || bx == G.n[0])) ? 1 : 0) |
                          ((G.per[1] && (by == 1 || by == G.n[1])) ? 2 : 0) | ((izi == 1 || izi == G.n[2]) ? 4 : 0);
-        S.lmeta[i] = izi | (edge << 16) | (min(c, 255) << 20);
+        rec.x = izi | (edge << 16) | (min(c, 255) << 20);
+        S.lrec[i] = rec;
         if (c > kNbrCap) ++over;
     }
     if (over) atomicAdd(&S.lctl->overflow, over);
@@ -289,9 +295,9 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
 // frozen-frame offsets, FP64 position accumulation; the periodic wrap and
 // the domain test (FP64 compares) only run for slots whose frozen bin is on
 // a face, the only ones that can cross it before the next build.
-// Each block takes a contiguous chunk of slots (one wave of blocks covers
-// all slots), so a thread's colony changes rarely and is found by stepping
-// forward from the last one instead of a binary search per slot.
+// Each block takes a contiguous chunk of slots, so a thread's colony is
+// found by one binary search and then by stepping forward from the last one.
+// The list metadata and the first entries come in one 16-byte record.
 // (256, 6): 40 registers, six blocks per SM; the kernel is latency bound and
 // gains more from the resident warps than it loses to the few spills
 __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
@@ -303,122 +309,156 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
     const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
     const float4 *__restrict__ rel_a = S.rel[a];
     const int *__restrict__ nbr = S.nbr;
-    // smallest and largest increment per component (order-preserving keys)
-    unsigned kmin[3] = {kKeyPosInf, kKeyPosInf, kKeyPosInf}, kmax[3] = {kKeyNegInf, kKeyNegInf, kKeyNegInf};
+    // smallest and largest increment per component (order-preserving keys),
+    // per warp in shared memory: reduced over the warp after each pass, so
+    // that no register holds them through the list walk
+    __shared__ unsigned wmin[32][3], wmax[32][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane < 3) {
+        wmin[w][lane] = kKeyPosInf;
+        wmax[w][lane] = kKeyNegInf;
+    }
+    __syncwarp();
     const int i0 = blockIdx.x * chunk;
     const int i1 = min(i0 + chunk, n);
     int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.geoms, S.ncol, i0 + threadIdx.x) : 0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        while (colony + 1 < S.ncol && __ldg(&S.geoms[colony].slot_end) <= i) ++colony;
-        const DevGeom &G = S.geoms[colony];
-        const float4 me = rel_a[i];
-        const int meta = S.lmeta[i];
-        const int izi = meta & 0xffff;
-        const int edge = (meta >> 16) & 7;
-        const int cnt = meta >> 20;
-        const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
-        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-        auto pair = [&](const float4 q, float ox, float oy, float oz) {
-            const float ex = (me.x - q.x) - ox;
-            const float ey = (me.y - q.y) - oy;
-            const float ez = (me.z - q.z) - oz;
-            const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float rSf = __fadd_rn(me.w, q.w);
-            const float rAf = __fadd_rn(rSf, bwf);
-            if (!(r2f < __fmul_rn(rAf, rAf))) return;
-            const float inv = rsqrtf(r2f);
-            const float rn = __fmul_rn(r2f, inv);
-            const float d1 = __fsub_rn(rn, rAf);
-            const float F = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
-            const float Fi = __fmul_rn(F, inv);
-            gx = __fmaf_rn(Fi, ex, gx);
-            gy = __fmaf_rn(Fi, ey, gy);
-            gz = __fmaf_rn(Fi, ez, gz);
-        };
-        if (cnt <= kNbrCap) {
-            auto entry = [&](unsigned e, const float4 q) {
-                const unsigned code = e >> kNbrShift;
-                pair(q, shift_of(code & 3u, dxb), shift_of((code >> 2) & 3u, dyb), shift_of((code >> 4) & 3u, dzb));
+    for (int base = i0; base < i1; base += blockDim.x) {  // same trip count for every thread
+        const int i = base + threadIdx.x;
+        unsigned lo0 = kKeyPosInf, lo1 = kKeyPosInf, lo2 = kKeyPosInf;
+        unsigned hi0 = kKeyNegInf, hi1 = kKeyNegInf, hi2 = kKeyNegInf;
+        if (i < i1) {
+            while (colony + 1 < S.ncol && __ldg(&S.geoms[colony].slot_end) <= i) ++colony;
+            const DevGeom &G = S.geoms[colony];
+            const float4 me = rel_a[i];
+            const int4 rec = __ldg(&S.lrec[i]);
+            const int meta = rec.x;
+            const int izi = meta & 0xffff;
+            const int edge = (meta >> 16) & 7;
+            const int cnt = meta >> 20;
+            const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
+            float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+            auto pair = [&](const float4 q, float ox, float oy, float oz) {
+                const float ex = (me.x - q.x) - ox;
+                const float ey = (me.y - q.y) - oy;
+                const float ez = (me.z - q.z) - oz;
+                const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+                const float rSf = __fadd_rn(me.w, q.w);
+                const float rAf = __fadd_rn(rSf, bwf);
+                if (!(r2f < __fmul_rn(rAf, rAf))) return;
+                const float inv = rsqrtf(r2f);
+                const float rn = __fmul_rn(r2f, inv);
+                const float d1 = __fsub_rn(rn, rAf);
+                const float F = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
+                const float Fi = __fmul_rn(F, inv);
+                gx = __fmaf_rn(Fi, ex, gx);
+                gy = __fmaf_rn(Fi, ey, gy);
+                gz = __fmaf_rn(Fi, ez, gz);
             };
-            const int *col = nbr + i;
-            int k = 0;
-            // four entries in flight at a time: the list loads and the
-            // neighbour gathers are independent across entries
-            for (; k + 4 <= cnt; k += 4) {
-                const unsigned e0 = (unsigned)__ldg(col + (size_t)k * n);
-                const unsigned e1 = (unsigned)__ldg(col + (size_t)(k + 1) * n);
-                const unsigned e2 = (unsigned)__ldg(col + (size_t)(k + 2) * n);
-                const unsigned e3 = (unsigned)__ldg(col + (size_t)(k + 3) * n);
-                const float4 q0 = __ldg(&rel_a[e0 & kSlotMask]);
-                const float4 q1 = __ldg(&rel_a[e1 & kSlotMask]);
-                const float4 q2 = __ldg(&rel_a[e2 & kSlotMask]);
-                const float4 q3 = __ldg(&rel_a[e3 & kSlotMask]);
-                entry(e0, q0);
-                entry(e1, q1);
-                entry(e2, q2);
-                entry(e3, q3);
+            if (cnt <= kNbrCap) {
+                auto entry = [&](unsigned e, const float4 q) {
+                    const unsigned code = e >> kNbrShift;
+                    pair(q, shift_of(code & 3u, dxb), shift_of((code >> 2) & 3u, dyb), shift_of((code >> 4) & 3u, dzb));
+                };
+                // the first entries came with the metadata: their gathers go out
+                // together, one round trip for the typical short list
+                const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                const float4 p0 = (cnt > 0) ? __ldg(&rel_a[(unsigned)rec.y & kSlotMask]) : z4;
+                const float4 p1 = (cnt > 1) ? __ldg(&rel_a[(unsigned)rec.z & kSlotMask]) : z4;
+                const float4 p2 = (cnt > 2) ? __ldg(&rel_a[(unsigned)rec.w & kSlotMask]) : z4;
+                if (cnt > 0) entry((unsigned)rec.y, p0);
+                if (cnt > 1) entry((unsigned)rec.z, p1);
+                if (cnt > 2) entry((unsigned)rec.w, p2);
+                const int *col = nbr + i;  // entry k in plane k - kNbrInline
+                int k = kNbrInline;
+                // four entries in flight at a time: the list loads and the
+                // neighbour gathers are independent across entries
+                for (; k + 4 <= cnt; k += 4) {
+                    const unsigned e0 = (unsigned)__ldg(col + (size_t)(k - kNbrInline) * n);
+                    const unsigned e1 = (unsigned)__ldg(col + (size_t)(k + 1 - kNbrInline) * n);
+                    const unsigned e2 = (unsigned)__ldg(col + (size_t)(k + 2 - kNbrInline) * n);
+                    const unsigned e3 = (unsigned)__ldg(col + (size_t)(k + 3 - kNbrInline) * n);
+                    const float4 q0 = __ldg(&rel_a[e0 & kSlotMask]);
+                    const float4 q1 = __ldg(&rel_a[e1 & kSlotMask]);
+                    const float4 q2 = __ldg(&rel_a[e2 & kSlotMask]);
+                    const float4 q3 = __ldg(&rel_a[e3 & kSlotMask]);
+                    entry(e0, q0);
+                    entry(e1, q1);
+                    entry(e2, q2);
+                    entry(e3, q3);
+                }
+                for (; k < cnt; ++k) {
+                    const unsigned e = (unsigned)__ldg(col + (size_t)(k - kNbrInline) * n);
+                    entry(e, __ldg(&rel_a[e & kSlotMask]));
+                }
+            } else {  // list overflow: walk the frozen cells with the current offsets
+                int bx, by;
+                col_to_bxy(G, S.col[B][i], bx, by);
+                visit_cells(S, G, S.rank[B][i], bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
+                    pair(__ldg(&S.rel[a][__ldg(&S.perm[B][u])]), (float)dxs * dxb, (float)dys * dyb,
+                         (float)dzs * dzb);
+                });
             }
-            for (; k < cnt; ++k) {
-                const unsigned e = (unsigned)__ldg(col + (size_t)k * n);
-                entry(e, __ldg(&rel_a[e & kSlotMask]));
+            float dzw;
+            if (izi < G.nwz) {
+                const float2 c = G.wz[izi];
+                dzw = (c.x + me.z) + c.y;
+            } else {
+                dzw = (float)(S.z[a][i] - P.z_wall);
             }
-        } else {  // list overflow: walk the frozen cells with the current offsets
-            int bx, by;
-            col_to_bxy(G, S.col[B][i], bx, by);
-            visit_cells(S, G, S.rank[B][i], bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
-                pair(__ldg(&S.rel[a][__ldg(&S.perm[B][u])]), (float)dxs * dxb, (float)dys * dyb,
-                     (float)dzs * dzb);
-            });
+            const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, me.w, zkf, zbwf, zgf);
+            const float ix = dtf * vx, iy = dtf * vy, iz = dtf * vz;
+            double nx = S.x[a][i] + f2d_int(ix);
+            double ny = S.y[a][i] + f2d_int(iy);
+            const double nz = S.z[a][i] + f2d_int(iz);
+            if (edge) {
+                if (edge & 1) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
+                if (edge & 2) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+                if ((edge & 4) && !(nz >= G.plo[2] && nz < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+            }
+            S.x[b][i] = nx;
+            S.y[b][i] = ny;
+            S.z[b][i] = nz;
+            S.rel[b][i] = make_float4(me.x + ix, me.y + iy, me.z + iz, me.w);
+            S.vxf[i] = vx;
+            S.vyf[i] = vy;
+            S.vzf[i] = vz;
+            lo0 = hi0 = fkey(ix);
+            lo1 = hi1 = fkey(iy);
+            lo2 = hi2 = fkey(iz);
+            if (!isfinite(ix + iy + iz)) {
+                atomicAdd(&S.cnt->nonfinite, 1ULL);
+                lo0 = 0u;  // spreads the bound: the next step rebuilds
+                hi0 = 0xffffffffu;
+            }
         }
-        float dzw;
-        if (izi < G.nwz) {
-            const float2 c = G.wz[izi];
-            dzw = (c.x + me.z) + c.y;
-        } else {
-            dzw = (float)(S.z[a][i] - P.z_wall);
-        }
-        const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, me.w, zkf, zbwf, zgf);
-        const float ix = dtf * vx, iy = dtf * vy, iz = dtf * vz;
-        double nx = S.x[a][i] + f2d_int(ix);
-        double ny = S.y[a][i] + f2d_int(iy);
-        const double nz = S.z[a][i] + f2d_int(iz);
-        if (edge) {
-            if (edge & 1) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
-            if (edge & 2) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
-            if ((edge & 4) && !(nz >= G.plo[2] && nz < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
-        }
-        S.x[b][i] = nx;
-        S.y[b][i] = ny;
-        S.z[b][i] = nz;
-        S.rel[b][i] = make_float4(me.x + ix, me.y + iy, me.z + iz, me.w);
-        S.vxf[i] = vx;
-        S.vyf[i] = vy;
-        S.vzf[i] = vz;
-        if (!isfinite(ix + iy + iz)) {
-            atomicAdd(&S.cnt->nonfinite, 1ULL);
-            kmin[0] = 0u;  // spreads the bound: the next step rebuilds
-            kmax[0] = 0xffffffffu;
-        }
-        const unsigned k0 = fkey(ix), k1 = fkey(iy), k2 = fkey(iz);
-        kmin[0] = min(kmin[0], k0);
-        kmax[0] = max(kmax[0], k0);
-        kmin[1] = min(kmin[1], k1);
-        kmax[1] = max(kmax[1], k1);
-        kmin[2] = min(kmin[2], k2);
-        kmax[2] = max(kmax[2], k2);
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            kmin[k] = min(kmin[k], __shfl_xor_sync(0xffffffffu, kmin[k], o));
-            kmax[k] = max(kmax[k], __shfl_xor_sync(0xffffffffu, kmax[k], o));
+        lo0 = __reduce_min_sync(0xffffffffu, lo0);
+        hi0 = __reduce_max_sync(0xffffffffu, hi0);
+        lo1 = __reduce_min_sync(0xffffffffu, lo1);
+        hi1 = __reduce_max_sync(0xffffffffu, hi1);
+        lo2 = __reduce_min_sync(0xffffffffu, lo2);
+        hi2 = __reduce_max_sync(0xffffffffu, hi2);
+        if (lane == 0) {
+            wmin[w][0] = min(wmin[w][0], lo0);
+            wmax[w][0] = max(wmax[w][0], hi0);
+            wmin[w][1] = min(wmin[w][1], lo1);
+            wmax[w][1] = max(wmax[w][1], hi1);
+            wmin[w][2] = min(wmin[w][2], lo2);
+            wmax[w][2] = max(wmax[w][2], hi2);
         }
     }
-    if ((threadIdx.x & 31) == 0 && kmax[0] >= kmin[0]) {
-        for (int k = 0; k < 3; ++k) {
-            atomicMin(&S.lctl->inc_min[k], kmin[k]);
-            atomicMax(&S.lctl->inc_max[k], kmax[k]);
+    // then over the block: six atomics per block, not per warp (updates of
+    // one address serialise in its L2 slice)
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        unsigned lo = kKeyPosInf, hi = kKeyNegInf;
+        for (int v = 0; v < nw; ++v) {
+            lo = min(lo, wmin[v][k]);
+            hi = max(hi, wmax[v][k]);
+        }
+        if (hi >= lo) {
+            atomicMin(&S.lctl->inc_min[k], lo);
+            atomicMax(&S.lctl->inc_max[k], hi);
         }
     }
 }
@@ -446,12 +486,12 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block,
                      cudaStream_t st)
 {
-    // grid = the SM count; one wave of resident blocks, each a chunk of slots
-    static int occ = 0;
-    if (occ == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_list_step, block, 0) != cudaSuccess) occ = 1;
-    const int want = grid * std::max(occ, 1);
-    int chunk = (S.n + want - 1) / want;
-    chunk = ((chunk + block - 1) / block) * block;
+    // two passes of the block per chunk: short enough that the block
+    // scheduler evens out the uneven list lengths of the colonies (one wave
+    // of long chunks ends on its slowest block), long enough to amortise the
+    // colony search and the block's reduction of the increment spreads
+    (void)grid;
+    const int chunk = 2 * block;
     k_list_step<<<(S.n + chunk - 1) / chunk, block, 0, st>>>(S, P, (float)dt, a, chunk);
     return 1;
 }
