@@ -764,8 +764,7 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
     const DevState &S = ctx->S;
     cudaStream_t st = ctx->stream;
     const DevParams P = dev_params(ctx->prm);
-    CK(cudaMemsetAsync(ctx->d_cnt, 0, offsetof(DevCounters, nonfinite), st));
-    CK(cudaMemsetAsync(&ctx->d_cnt->pairs, 0, sizeof(DevCounters) - offsetof(DevCounters, pairs), st));
+    // the decision kernel clears the per-step counters
     const int64_t n = ctx->n;
     const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
     if (ctx->capturing) {

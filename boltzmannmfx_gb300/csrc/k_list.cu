@@ -67,8 +67,14 @@ constexpr unsigned kKeyNegInf = 0x007fffffu;  // fkey(-inf)
 // drift common to all slots (here: the rise of the slots below the growth
 // surface).  Each step adds eps_step per component for the FP32 rounding of
 // the offset updates.
-__global__ void k_list_decide(ListCtl *c, cudaGraphConditionalHandle h, int use_h)
+// It also clears the per-step counters (no memset nodes in the step).
+__global__ void k_list_decide(ListCtl *c, DevCounters *cnt, cudaGraphConditionalHandle h, int use_h)
 {
+    cnt->out_of_domain = 0ull;
+    cnt->edge_ghost = 0ull;
+    cnt->pairs = 0ull;
+    cnt->bond_repairs = 0ull;
+    cnt->moved = 0ull;
     float r2 = 0.0f;
     float rg[3];
     for (int k = 0; k < 3; ++k) {
@@ -467,7 +473,7 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
 
 int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond, cudaStream_t st)
 {
-    k_list_decide<<<1, 1, 0, st>>>(S.lctl, (cudaGraphConditionalHandle)cond, use_cond);
+    k_list_decide<<<1, 1, 0, st>>>(S.lctl, S.cnt, (cudaGraphConditionalHandle)cond, use_cond);
     return 1;
 }
 
