@@ -191,8 +191,14 @@ int grid_for(bmxg_ctx *ctx, const Shape &s, int64_t n)
 
 DevParams dev_params(const bmxg_params &p)
 {
-    return DevParams{p.bndry_width, p.stiffness,     p.z_wall,      p.z_bndry_width, p.z_stiffness,
-                     p.z_gravity,   p.bond_strength, p.bond_cutoff, p.viscosity,     p.neighborhood};
+    DevParams d{p.bndry_width, p.stiffness,     p.z_wall,      p.z_bndry_width, p.z_stiffness,
+                p.z_gravity,   p.bond_strength, p.bond_cutoff, p.viscosity,     p.neighborhood};
+    d.bw32 = (float)d.bw;
+    d.k32 = (float)d.k;
+    d.z_k32 = (float)d.z_k;
+    d.z_bw32 = (float)d.z_bw;
+    d.z_g32 = (float)d.z_g;
+    return d;
 }
 
 int check_params(const bmxg_params *p)

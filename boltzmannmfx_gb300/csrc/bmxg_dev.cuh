@@ -66,6 +66,9 @@ struct DevCounters {
 // Force parameters, fpar[0..8] (src/chemistry/bmx_cell_interaction.cpp:84-93).
 struct DevParams {
     double bw, k, z_wall, z_bw, z_k, z_g, k_bond, bond_cutoff, visc, nbh;
+    // bw, k, z_k, z_bw, z_g rounded to FP32 on the host for the FP32F list
+    // kernels (a conversion per thread is an FP64-pipe instruction)
+    float bw32, k32, z_k32, z_bw32, z_g32;
 };
 
 // Bin index along one axis in the coordinates of the box grown by one cell:

@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
     const int n = S.n;
-    const float reach = (float)P.bw + S.lctl->skin;
+    const float reach = P.bw32 + S.lctl->skin;
     unsigned long long over = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int i = S.perm[B][t];
@@ -311,8 +311,8 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
     constexpr int B = kListBins;
     const int b = a ^ 1;
     const int n = S.n;
-    const float bwf = (float)P.bw, kf = (float)P.k;
-    const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
+    const float bwf = P.bw32, kf = P.k32;
+    const float zkf = P.z_k32, zbwf = P.z_bw32, zgf = P.z_g32;
     const float4 *__restrict__ rel_a = S.rel[a];
     const int *__restrict__ nbr = S.nbr;
     // smallest and largest increment per component (order-preserving keys),
