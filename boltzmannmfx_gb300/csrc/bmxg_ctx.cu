@@ -106,6 +106,16 @@ struct bmxg_ctx {
     unsigned long long body_runs_seen = 0;  // list builds already counted as launches
     bool capturing = false;       // enqueue_step runs inside a graph capture
     cudaStream_t body_stream = nullptr;     // captures the bodies of conditional nodes
+
+    // loads and stores of host arrays: the copies run on io_stream, overlapped
+    // with the sort, gather and scatter kernels on `stream`; the device
+    // staging is kept (and grown) across calls
+    cudaStream_t io_stream = nullptr;
+    cudaEvent_t io_ev[6] = {};
+    char *io_buf = nullptr;
+    size_t io_cap = 0;
+    unsigned long long *d_chk = nullptr;    // state-check flags (4), device
+    unsigned long long *h_chk = nullptr;    // and pinned host
 };
 
 namespace {
@@ -160,6 +170,30 @@ void free_adjoint(bmxg_ctx *ctx)
     ctx->lam[0] = ctx->lam[1] = nullptr;
     ctx->traj_T = -1;
 }
+
+// Device staging of at least `bytes` for host loads and stores.
+int ensure_io(bmxg_ctx *ctx, size_t bytes)
+{
+    if (bytes <= ctx->io_cap) return BMXG_OK;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamSynchronize(ctx->io_stream));
+    if (ctx->io_buf) cudaFree(ctx->io_buf);
+    ctx->io_buf = nullptr;
+    ctx->io_cap = 0;
+    CK(cudaMalloc(&ctx->io_buf, bytes));
+    ctx->io_cap = bytes;
+    return BMXG_OK;
+}
+
+// Waits for the load / store copies still reading or writing caller memory
+// when a call returns early.
+struct JoinIo {
+    cudaStream_t s;
+    ~JoinIo()
+    {
+        if (s) cudaStreamSynchronize(s);
+    }
+};
 
 void free_state(bmxg_ctx *ctx)
 {
@@ -253,6 +287,8 @@ void build_geoms(bmxg_ctx *ctx)
             G.dx[d] = G.len[d] / (double)G.n[d];
             G.dxi[d] = 1.0 / G.dx[d];
             G.dxf[d] = (float)G.dx[d];
+            G.plof[d] = (float)G.plo[d];
+            G.dxif[d] = (float)G.dxi[d];
             G.per[d] = g.is_periodic[d] ? 1 : 0;
             diag2 += 4.0 * G.dx[d] * G.dx[d];
         }
@@ -317,6 +353,11 @@ int bmxg_create(const bmxg_params *params, int32_t ncolonies, const bmxg_geometr
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_cnt, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_lctl, sizeof(ListCtl));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->body_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking);
+    for (cudaEvent_t &ev : ctx->io_ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_chk, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_chk, 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         ctx->err = cudaGetErrorString(e);
         bmxg_destroy(ctx);
@@ -339,6 +380,15 @@ void bmxg_destroy(bmxg_ctx *ctx)
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
     if (ctx->h_lctl) cudaFreeHost(ctx->h_lctl);
     if (ctx->body_stream) cudaStreamDestroy(ctx->body_stream);
+    if (ctx->io_stream) {
+        cudaStreamSynchronize(ctx->io_stream);
+        cudaStreamDestroy(ctx->io_stream);
+    }
+    for (cudaEvent_t ev : ctx->io_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->io_buf) cudaFree(ctx->io_buf);
+    if (ctx->d_chk) cudaFree(ctx->d_chk);
+    if (ctx->h_chk) cudaFreeHost(ctx->h_chk);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
@@ -394,33 +444,48 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
             if (off[c + 1] < off[c]) return fail(ctx, BMXG_ERR_ARG, "colony_offsets must not decrease");
     }
     const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    // Positions, radii and cell types: read in place from device arrays; host
+    // arrays go to the staging, radii and cell types first on the compute
+    // stream (the state check needs them), positions on the copy stream, so
+    // that their copy overlaps the check and the host's decisions below.
+    const double *src_x = p->x, *src_y = p->y, *src_z = p->z, *src_r = p->radius;
+    const int *src_ct = p->cell_type;
+    JoinIo join{nullptr};
+    cudaStream_t st0 = ctx->stream, st1 = ctx->io_stream;
+    if (n && where == BMXG_HOST) {
+        int rc0 = ensure_io(ctx, (size_t)n * 36 + 256);
+        if (rc0) return rc0;
+        double *bx = (double *)ctx->io_buf, *by = bx + n, *bz = by + n, *br = bz + n;
+        int *bct = (int *)(br + n);
+        CK(cudaEventRecord(ctx->io_ev[0], st0));  // earlier kernels on st0 are done with the staging
+        CK(cudaStreamWaitEvent(st1, ctx->io_ev[0], 0));
+        join.s = st1;
+        CK(cudaMemcpyAsync(br, p->radius, sizeof(double) * n, kind, st0));
+        CK(cudaMemcpyAsync(bct, p->cell_type, sizeof(int) * n, kind, st0));
+        CK(cudaMemcpyAsync(bx, p->x, sizeof(double) * n, kind, st1));
+        CK(cudaMemcpyAsync(by, p->y, sizeof(double) * n, kind, st1));
+        CK(cudaMemcpyAsync(bz, p->z, sizeof(double) * n, kind, st1));
+        CK(cudaEventRecord(ctx->io_ev[1], st1));
+        src_x = bx;
+        src_y = by;
+        src_z = bz;
+        src_r = br;
+        src_ct = bct;
+    }
     // cell types decide which path runs (rods need their fields) and the
-    // largest radius whether the FP32F list is exact: checked on the device
-    // (the arrays go there anyway), one small read-back
+    // largest radius whether the FP32F list is exact: checked on the device,
+    // one small read-back
     bool rods = false;
     double rmax = 0.0;
     if (n) {
-        cudaStream_t st0 = ctx->stream;
-        unsigned long long *chk = nullptr;
-        int *dct = nullptr;
-        double *dr = nullptr;
-        unsigned long long h[4] = {0, 0, 0, 0};
-        CK(cudaMallocAsync((void **)&chk, sizeof(h) + sizeof(int) * n + sizeof(double) * n + 64, st0));
-        dr = (double *)((char *)chk + 64);
-        dct = (int *)(dr + n);
-        cudaError_t e = cudaMemsetAsync(chk, 0, sizeof(h), st0);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dct, p->cell_type, sizeof(int) * n, kind, st0);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dr, p->radius, sizeof(double) * n, kind, st0);
-        if (e == cudaSuccess) {
-            Shape sh;
-            launch_check_state(dct, dr, (int)n, chk, grid_for(ctx, sh, n), sh.block, st0);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(h, chk, sizeof(h), cudaMemcpyDeviceToHost, st0);
-        cudaFreeAsync(chk, st0);
-        const cudaError_t e2 = cudaStreamSynchronize(st0);
-        if (e == cudaSuccess) e = e2;
+        CK(cudaMemsetAsync(ctx->d_chk, 0, 4 * sizeof(unsigned long long), st0));
+        Shape sh;
+        launch_check_state(src_ct, src_r, (int)n, ctx->d_chk, grid_for(ctx, sh, n), sh.block, st0);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(ctx->h_chk, ctx->d_chk, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st0));
+        const cudaError_t e = cudaStreamSynchronize(st0);
         if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("state check: ") + cudaGetErrorString(e));
+        const unsigned long long *h = ctx->h_chk;
         if (h[0]) return fail(ctx, BMXG_ERR_ARG, "cell_type must be 0 or 1");
         rods = h[1] != 0;
         const uint64_t rb = h[2];
@@ -493,19 +558,16 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     }
     const int blk = ctx->sh_misc.block;
     const int grd = grid_for(ctx, ctx->sh_misc, n);
-    // caller-order positions into the slot x/y/z of buffer 1 (scratch for now)
-    CK(cudaMemcpyAsync(S.x[1], p->x, sizeof(double) * n, kind, st));
-    CK(cudaMemcpyAsync(S.y[1], p->y, sizeof(double) * n, kind, st));
-    CK(cudaMemcpyAsync(S.z[1], p->z, sizeof(double) * n, kind, st));
+    if (join.s) CK(cudaStreamWaitEvent(st, ctx->io_ev[1], 0));  // staged positions
     // canonical order of the caller's particles
-    LAUNCH(launch_user_bin(S, S.x[1], S.y[1], S.z[1], S.col[1], S.iz[1], grd, blk, st));
+    LAUNCH(launch_user_bin(S, src_x, src_y, src_z, S.col[1], S.iz[1], grd, blk, st));
     LAUNCH(launch_scan(S.colcnt, S.colstart[1], (int)ncols, ctx->scan_scratch, st));
     LAUNCH(launch_user_scatter_canon(S, S.col[1], S.iz[1], S.colstart[1], ctx->uperm, grd, blk, st));
     CK(cudaMemcpyAsync(S.orig, ctx->uperm, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
     // gather every field into slot order
-    LAUNCH(launch_gather_d(S.x[0], S.x[1], ctx->uperm, (int)n, grd, blk, st));
-    LAUNCH(launch_gather_d(S.y[0], S.y[1], ctx->uperm, (int)n, grd, blk, st));
-    LAUNCH(launch_gather_d(S.z[0], S.z[1], ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.x[0], src_x, ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.y[0], src_y, ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.z[0], src_z, ctx->uperm, (int)n, grd, blk, st));
     auto up_d = [&](const double *src, double *dst, double fill) -> int {
         if (src) {
             CK(cudaMemcpyAsync(ctx->ud, src, sizeof(double) * n, kind, st));
@@ -529,9 +591,8 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         }
         return BMXG_OK;
     };
-    if ((rc = up_d(p->radius, S.rad, 0.0))) return rc;
-    CK(cudaMemcpyAsync(ctx->ui, p->cell_type, sizeof(int) * n, kind, st));
-    LAUNCH(launch_gather_i8(S.ctype, ctx->ui, ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_d(S.rad, src_r, ctx->uperm, (int)n, grd, blk, st));
+    LAUNCH(launch_gather_i8(S.ctype, src_ct, ctx->uperm, (int)n, grd, blk, st));
     if ((rc = up_d(p->velx, S.vx, 0.0))) return rc;
     if ((rc = up_d(p->vely, S.vy, 0.0))) return rc;
     if ((rc = up_d(p->velz, S.vz, 0.0))) return rc;
@@ -592,30 +653,64 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     const int64_t n = ctx->n;
     if (n == 0) return BMXG_OK;
     const DevState &S = ctx->S;
-    cudaStream_t st = ctx->stream;
-    const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    cudaStream_t st = ctx->stream, st1 = ctx->io_stream;
+    const bool host = where == BMXG_HOST;
     const int blk = ctx->sh_misc.block;
     const int grd = grid_for(ctx, ctx->sh_misc, n);
     const int a = ctx->parity;
-    // one staging buffer per kind: the stream orders each copy before the
-    // next scatter into it; one synchronisation at the end
+    // Device arrays receive the caller-order scatter directly.  Host arrays:
+    // each field is scattered into one of two staging halves on the compute
+    // stream and copied out on the copy stream, so that the copy of one field
+    // overlaps the scatter of the next.
+    JoinIo join{nullptr};
+    int used = 0;
+    if (host) {
+        int rc0 = ensure_io(ctx, (size_t)n * 48 + 256);
+        if (rc0) return rc0;
+        CK(cudaEventRecord(ctx->io_ev[0], st));
+        CK(cudaStreamWaitEvent(st1, ctx->io_ev[0], 0));
+        join.s = st1;
+    }
+    char *half[2] = {ctx->io_buf, ctx->io_buf + (size_t)n * 24 + 128};
+    // destination of the next field: the caller's array or a staging half
+    cudaError_t wait_err = cudaSuccess;
+    auto begin = [&](void *dst) -> void * {
+        if (!host) return dst;
+        const int h = used & 1;
+        if (used >= 2) {  // the half's previous copy-out is done
+            const cudaError_t e = cudaStreamWaitEvent(st, ctx->io_ev[4 + h], 0);
+            if (e != cudaSuccess) wait_err = e;
+        }
+        return half[h];
+    };
+    auto finish = [&](void *dst, size_t bytes) -> int {
+        if (!host) return BMXG_OK;
+        CK(wait_err);
+        const int h = used & 1;
+        CK(cudaEventRecord(ctx->io_ev[2 + h], st));
+        CK(cudaStreamWaitEvent(st1, ctx->io_ev[2 + h], 0));
+        CK(cudaMemcpyAsync(dst, half[h], bytes, cudaMemcpyDeviceToHost, st1));
+        CK(cudaEventRecord(ctx->io_ev[4 + h], st1));
+        ++used;
+        return BMXG_OK;
+    };
     auto out_d = [&](double *dst, const double *src) -> int {
         if (!dst || !src) return BMXG_OK;
-        LAUNCH(launch_scatter_d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
-        CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
-        return BMXG_OK;
+        double *o = (double *)begin(dst);
+        LAUNCH(launch_scatter_d(o, src, S.orig, (int)n, grd, blk, st));
+        return finish(dst, sizeof(double) * n);
     };
     auto out_i = [&](int32_t *dst, const int *src, int planes) -> int {
         if (!dst || !src) return BMXG_OK;
-        LAUNCH(launch_scatter_i(ctx->ui, src, S.orig, (int)n, planes, grd, blk, st));
-        CK(cudaMemcpyAsync(dst, ctx->ui, sizeof(int) * n * planes, kind, st));
-        return BMXG_OK;
+        int *o = (int *)begin(dst);
+        LAUNCH(launch_scatter_i(o, src, S.orig, (int)n, planes, grd, blk, st));
+        return finish(dst, sizeof(int) * n * planes);
     };
     auto out_f = [&](double *dst, const float *src) -> int {  // FP32F velocities, widened
         if (!dst || !src) return BMXG_OK;
-        LAUNCH(launch_scatter_f2d(ctx->ud, src, S.orig, (int)n, grd, blk, st));
-        CK(cudaMemcpyAsync(dst, ctx->ud, sizeof(double) * n, kind, st));
-        return BMXG_OK;
+        double *o = (double *)begin(dst);
+        LAUNCH(launch_scatter_f2d(o, src, S.orig, (int)n, grd, blk, st));
+        return finish(dst, sizeof(double) * n);
     };
     int rc;
     if ((rc = out_d(p->x, S.x[a]))) return rc;
@@ -655,6 +750,7 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
             if (f) CK(cudaMemsetAsync(f, 0, sizeof(int32_t) * n, st));
     }
     CK(cudaStreamSynchronize(st));
+    if (host) CK(cudaStreamSynchronize(st1));
     return BMXG_OK;
 }
 
@@ -854,13 +950,13 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
         return BMXG_OK;
     }
     // kResyncEvery steps (an even number, so the graph ends on the parity it
-    // starts from); the FP32F re-sync falls on its first step
+    // starts from); the FP32F re-sync falls on its last step
     cudaGraph_t g = nullptr;
     const int64_t before = ctx->launches;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc2 = BMXG_OK;
     ctx->capturing = true;
-    for (int s = 0; s < kResyncEvery && !rc2; ++s) rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == 0);
+    for (int s = 0; s < kResyncEvery && !rc2; ++s) rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == kResyncEvery - 1);
     ctx->capturing = false;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc2) {
@@ -914,7 +1010,10 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     int32_t left = nsteps;
     ctx->kev_used = 0;
     auto eager = [&]() -> int {  // one step outside a graph, on the re-sync schedule
-        int rc = enqueue_step(ctx, subdt, precision, ctx->parity, ctx->step_count % kResyncEvery == 0);
+        // re-sync on the last step of each kResyncEvery (not right after a load,
+        // whose offsets are exact)
+        int rc = enqueue_step(ctx, subdt, precision, ctx->parity,
+                              ctx->step_count % kResyncEvery == kResyncEvery - 1);
         if (rc) return rc;
         ctx->parity ^= 1;
         ++ctx->step_count;

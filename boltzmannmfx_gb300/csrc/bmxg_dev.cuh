@@ -36,6 +36,7 @@ constexpr int kResyncEvery = 8;                 // FP32F: exact FP64 re-binning 
 struct DevGeom {
     double plo[3], phi[3], len[3], dx[3], dxi[3];
     float dxf[3];
+    float plof[3], dxif[3];  // plo and dxi rounded to FP32 (bin_of_fast; 0: not set, FP64 binning)
     int n[3];
     int per[3];
     int col_base;       // first global column of this colony
@@ -81,6 +82,38 @@ __device__ __forceinline__ int bin_of(double x, double plo, double dxi, int lo_c
     if (!(v > (double)lo_c)) return lo_c;
     if (v >= (double)hi_c + 1.0) return hi_c;
     return (int)v;
+}
+
+// Truncation of a double to FP32 from its bits (no FP64 instruction):
+// within |x| 2^-23 of x where |x| is in the normal FP32 range, 0 for a zero,
+// NaN otherwise (callers then take their FP64 path).
+__device__ __forceinline__ float d2f_trunc(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if ((b << 1) == 0ull) return 0.0f;
+    const unsigned hi = (unsigned)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+    if (e < -126 || e > 127) return __int_as_float(0x7fc00000);
+    return __uint_as_float((hi & 0x80000000u) | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
+// bin_of, exactly, mostly without FP64 arithmetic (GB300 issues FP64 at a
+// small fraction of the FP32 rate): v = (x - plo) dxi + 1 in FP32 from the
+// truncated x and the FP32 plo, dxi is within
+// 2^-20 ((|x| + |plo|) dxi + |v|) of the real value, which bounds the
+// truncation, the FP32 roundings and the FP64 formula's own roundings with
+// margin; when that interval holds no integer, the floor is the FP64
+// formula's, and the clamps of bin_of reduce to clamping the floor.
+// Otherwise (and for geometries without the FP32 values) bin_of itself.
+__device__ __forceinline__ int bin_of_fast(double x, double plo, double dxi, float plof, float dxif, int lo_c,
+                                           int hi_c)
+{
+    const float xf = d2f_trunc(x);
+    const float v = __fmaf_rn(__fsub_rn(xf, plof), dxif, 1.0f);
+    const float e = __fmul_rn(__fmaf_rn(fabsf(xf) + fabsf(plof), fabsf(dxif), fabsf(v)), 9.5367431640625e-07f);
+    const float f0 = floorf(__fsub_rn(v, e)), f1 = floorf(__fadd_rn(v, e));
+    if (f0 == f1 && dxif > 0.0f && fabsf(f0) < 1.0e7f) return min(max((int)f0, lo_c), hi_c);
+    return bin_of(x, plo, dxi, lo_c, hi_c);
 }
 
 // AMReX enforcePeriodic restated: shift by the domain length until inside,

@@ -151,9 +151,9 @@ __device__ __forceinline__ void rebin_slot_into(const DevState &S, const DevGeom
                                                 double z, double r, int bb, int rb, bool count_domain = true,
                                                 bool count_col = true)
 {
-    const int bx = bin_of(x, G.plo[0], G.dxi[0], 1, G.n[0]);
-    const int by = bin_of(y, G.plo[1], G.dxi[1], 1, G.n[1]);
-    const int bz = bin_of(z, G.plo[2], G.dxi[2], 1, G.n[2]);
+    const int bx = bin_of_fast(x, G.plo[0], G.dxi[0], G.plof[0], G.dxif[0], 1, G.n[0]);
+    const int by = bin_of_fast(y, G.plo[1], G.dxi[1], G.plof[1], G.dxif[1], 1, G.n[1]);
+    const int bz = bin_of_fast(z, G.plo[2], G.dxi[2], G.plof[2], G.dxif[2], 1, G.n[2]);
     place_slot(S, G, i, x, y, z, r, bb, rb, bx, by, bz, count_domain, count_col);
 }
 

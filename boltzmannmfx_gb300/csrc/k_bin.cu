@@ -159,9 +159,9 @@ __global__ void k_user_bin(const DevState S, const double *ux, const double *uy,
 {
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, u);  // colony slot ranges equal caller ranges
-        const int bx = bin_of(ux[u], G.plo[0], G.dxi[0], 1, G.n[0]);
-        const int by = bin_of(uy[u], G.plo[1], G.dxi[1], 1, G.n[1]);
-        const int bz = bin_of(uz[u], G.plo[2], G.dxi[2], 1, G.n[2]);
+        const int bx = bin_of_fast(ux[u], G.plo[0], G.dxi[0], G.plof[0], G.dxif[0], 1, G.n[0]);
+        const int by = bin_of_fast(uy[u], G.plo[1], G.dxi[1], G.plof[1], G.dxif[1], 1, G.n[1]);
+        const int bz = bin_of_fast(uz[u], G.plo[2], G.dxi[2], G.plof[2], G.dxif[2], 1, G.n[2]);
         const int c = column_of(G, bx, by);
         ucol[u] = c;
         uiz[u] = bz;

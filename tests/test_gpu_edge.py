@@ -56,6 +56,40 @@ def test_faces_and_corners(gpu_lib, oracle_lib):
     assert st["n_edge_ghost"] >= 0
 
 
+def test_bins_at_faces_exact(gpu_lib, oracle_lib):
+    """Positions on interior bin faces and up to three ulps either side, with
+    a shifted origin: the bins (an FP32 estimate where it is certain, FP64
+    otherwise) are the reference formula's, so the pair lists and the FP64
+    steps match the oracle bit for bit."""
+    rng = np.random.default_rng(11)
+    n_cell = (6, 5, 4)
+    lo = (-0.0031, 0.0017, 0.0)
+    hi = (lo[0] + 0.012, lo[1] + 0.010, 0.008)
+    g = Geometry.make(lo, hi, n_cell, (1, 1, 0))
+    P = configs.sphere_colony(300, 0.012, 0.010, rng, z_band=(0.0, 0.008))
+    P["x"] += lo[0]
+    P["y"] += lo[1]
+    for i in range(240):
+        d = i % 3
+        dx = (hi[d] - lo[d]) / n_cell[d]
+        v = lo[d] + int(rng.integers(1, n_cell[d])) * dx
+        off = int(rng.integers(-3, 4))
+        for _ in range(abs(off)):
+            v = np.nextafter(v, np.inf if off > 0 else -np.inf)
+        P["xyz"[d]][i] = v
+    prm = configs.deck_params()
+    ctx = Context(prm, g)
+    ctx.set_state(P)
+    assert same_pairs(ctx.pairs(), oracle_lib.pairs(prm, g, P))
+    ctx.step(0.25, 2, BMXG_FP64)
+    Q = P.copy()
+    ctx.get_state(Q)
+    R = P.copy()
+    oracle_lib.evolve(prm, [g], [0, P.n], R, 0.25, 2)
+    for k in ("x", "y", "z"):
+        assert np.array_equal(Q[k], R[k]), k
+
+
 def test_non_trivial_neighborhood_predicate(gpu_lib, oracle_lib):
     w = configs.sphere_plain()
     prm = w.params
