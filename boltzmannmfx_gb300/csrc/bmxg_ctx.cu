@@ -780,7 +780,7 @@ void prof_events(bmxg_ctx *ctx, cudaEvent_t *k0, cudaEvent_t *k1)
 // ---- FP32F neighbour list with a skin ---------------------------------------
 constexpr int kListMaxAge = 64;      // bounds the FP32 drift of the frozen-frame offsets
 constexpr int kListExactEvery = 8;   // builds between exact FP64 re-binnings
-constexpr int kListMinSteps = 2;     // shorter calls on a state without a list run the per-step path
+constexpr int kListMinSteps = 2;     // a shorter first call after a load runs the per-step path
 
 // Skin of the list for the loaded state and parameters, or 0 where the list
 // would not reproduce the reference's pair set: the largest cutoff
@@ -992,11 +992,11 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
     const double subdt = dt / 1.0;
     // FP32F spheres use the neighbour list wherever it reproduces the pair set,
-    // and where the calls are long enough to amortise a build: a call of
-    // fewer than kListMinSteps steps on a state without a valid list takes
-    // the per-step path
+    // and where the steps are many enough to amortise a build: the first call
+    // after a load, if shorter than kListMinSteps, takes the per-step path (a
+    // load-step-store caller never reuses a list); later calls build one
     float skin = (precision == BMXG_FP32F && ctx->list_mode) ? list_skin(ctx) : 0.0f;
-    if (skin > 0.0f && !ctx->list_valid && nsteps < kListMinSteps) skin = 0.0f;
+    if (skin > 0.0f && !ctx->list_valid && nsteps < kListMinSteps && ctx->step_count == 0) skin = 0.0f;
     if (skin > 0.0f) {
         int rc = ensure_list(ctx, skin);
         if (rc) return rc;

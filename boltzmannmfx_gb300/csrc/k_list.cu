@@ -495,9 +495,11 @@ int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, in
     // two passes of the block per chunk: short enough that the block
     // scheduler evens out the uneven list lengths of the colonies (one wave
     // of long chunks ends on its slowest block), long enough to amortise the
-    // colony search and the block's reduction of the increment spreads
-    (void)grid;
-    const int chunk = 2 * block;
+    // colony search and the block's reduction of the increment spreads.  One
+    // pass when two would leave fewer than four waves of six blocks per SM
+    // (grid = the SM count): small states need the blocks more.
+    const int two = (S.n + 2 * block - 1) / (2 * block);
+    const int chunk = (two >= 4 * 6 * grid) ? 2 * block : block;
     k_list_step<<<(S.n + chunk - 1) / chunk, block, 0, st>>>(S, P, (float)dt, a, chunk);
     return 1;
 }
