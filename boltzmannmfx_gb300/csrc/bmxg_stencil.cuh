@@ -55,13 +55,26 @@ __device__ __forceinline__ void visit_stencil(const DevState &S, const DevGeom &
     }
 }
 
+// First t in [lo, hi) with siz[t] >= v (siz ascends over the range).
+__device__ __forceinline__ int first_at_least(const int *__restrict__ siz, int lo, int hi, int v)
+{
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&siz[mid]) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // The same walk over the column-sorted copies (siz / srel, filled by the
 // rebuild): f(t, dxs, dys, dzs, sx, sy) gets the sorted index t of each
 // candidate (its slot is perm[t]).  An x-row's three columns by-1..by+1 are
 // consecutive column ids, so away from the periodic faces a row is three
 // back-to-back runs of one contiguous range; each run is ordered by z-bin
-// and stops at the first entry above izi + 1.  self_t = rank of the slot
-// itself.  Order of candidates: identical to visit_stencil.
+// and is entered by binary search at its first entry of z-bin izi - 1 (a
+// column can be many bins tall), and left at the first entry above izi + 1.
+// self_t = rank of the slot itself.  Order of candidates: identical to
+// visit_stencil.
 template <class F>
 __device__ __forceinline__ void visit_sorted(const DevState &S, const DevGeom &G, int a, int self_t, int bx,
                                              int by, int izi, F &&f)
@@ -84,7 +97,7 @@ __device__ __forceinline__ void visit_sorted(const DevState &S, const DevGeom &G
             int lo = __ldg(&cs[c]);
             for (int dys = -1; dys <= 1; ++dys) {
                 const int hi = __ldg(&cs[c + dys + 2]);
-                for (int t = lo; t < hi; ++t) {
+                for (int t = first_at_least(siz, lo, hi, izi - 1); t < hi; ++t) {
                     const int dzs = __ldg(&siz[t]) - izi;
                     if (dzs > 1) break;
                     if (dzs < -1 || t == self_t) continue;
@@ -97,7 +110,7 @@ __device__ __forceinline__ void visit_sorted(const DevState &S, const DevGeom &G
                 int cc, ssx, sy;
                 if (!stencil_row(G, ii, jj, cc, ssx, sy)) continue;
                 const int t1 = __ldg(&cs[cc + 1]);
-                for (int t = __ldg(&cs[cc]); t < t1; ++t) {
+                for (int t = first_at_least(siz, __ldg(&cs[cc]), t1, izi - 1); t < t1; ++t) {
                     const int dzs = __ldg(&siz[t]) - izi;
                     if (dzs > 1) break;
                     if (dzs < -1 || t == self_t) continue;
