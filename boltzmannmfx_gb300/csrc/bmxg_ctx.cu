@@ -54,6 +54,8 @@ struct bmxg_ctx {
     std::vector<void *> allocs;
     DevState S{};
     DevGeom *d_geoms = nullptr;
+    int *d_cbase = nullptr;                 // ncol + 1 colony slot offsets (device)
+    std::vector<int> h_cbase;
     std::vector<DevGeom> h_geoms;
     DevCounters *d_cnt = nullptr;
     DevCounters *h_cnt = nullptr;  // pinned
@@ -204,6 +206,7 @@ void free_state(bmxg_ctx *ctx)
     ctx->allocs.clear();
     ctx->S = DevState{};
     ctx->d_geoms = nullptr;
+    ctx->d_cbase = nullptr;
     ctx->scan_scratch = nullptr;
     ctx->cell_scratch = nullptr;
     ctx->ud = nullptr;
@@ -521,6 +524,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     } while (0)
     if (!reuse) {
     AL(ctx->d_geoms, ctx->ncol);
+    AL(ctx->d_cbase, ctx->ncol + 1);
     AL(ctx->d_cnt, 1);
     for (int k = 0; k < 2; ++k) {
         AL(S.x[k], n); AL(S.y[k], n); AL(S.z[k], n);
@@ -543,9 +547,12 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     }  // !reuse
 #undef AL
     S.geoms = ctx->d_geoms;
+    S.cbase = ctx->d_cbase;
     S.cnt = ctx->d_cnt;
     cudaStream_t st = ctx->stream;
     CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol, cudaMemcpyHostToDevice, st));
+    ctx->h_cbase.assign(off.begin(), off.end());
+    CK(cudaMemcpyAsync(ctx->d_cbase, ctx->h_cbase.data(), sizeof(int) * (ctx->ncol + 1), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
     CK(cudaMemsetAsync(S.colcnt, 0, sizeof(int) * std::max<int64_t>(ncols, 1), st));
     if (n == 0) {

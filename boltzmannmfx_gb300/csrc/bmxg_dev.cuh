@@ -131,13 +131,16 @@ __device__ __forceinline__ double wrap1(double x, double lo, double hi, double l
     return x;
 }
 
-__device__ __forceinline__ int colony_of(const DevGeom *geoms, int ncol, int slot)
+// Colony of a slot: binary search over the compact colony offsets (one
+// kilobyte for 256 colonies, resident in L1, where the geometry records are
+// ~0.7 KB apart).
+__device__ __forceinline__ int colony_of(const int *cbase, int ncol, int slot)
 {
     if (ncol == 1) return 0;
     int lo = 0, hi = ncol - 1;
-    while (lo < hi) {  // last colony whose slot_base <= slot
+    while (lo < hi) {  // last colony whose first slot <= slot
         int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&geoms[mid].slot_base) <= slot) lo = mid; else hi = mid - 1;
+        if (__ldg(&cbase[mid]) <= slot) lo = mid; else hi = mid - 1;
     }
     return lo;
 }

@@ -45,6 +45,7 @@ struct DevState {
     int ncol;          // colonies
     int ncols_total;   // columns over all colonies
     const DevGeom *geoms;
+    const int *cbase;  // ncol + 1: first slot of each colony, then n (a compact copy for colony lookups)
     DevCounters *cnt;
 
     double *x[2], *y[2], *z[2];

@@ -217,7 +217,7 @@ __device__ __forceinline__ float wall_law32(float dz, float rS, float zk, float 
 
 __device__ __forceinline__ const DevGeom &geom_of(const DevState &S, int i)
 {
-    return S.geoms[colony_of(S.geoms, S.ncol, i)];
+    return S.geoms[colony_of(S.cbase, S.ncol, i)];
 }
 
 }  // namespace bmxg

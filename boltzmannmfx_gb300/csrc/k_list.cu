@@ -327,13 +327,13 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
     __syncwarp();
     const int i0 = blockIdx.x * chunk;
     const int i1 = min(i0 + chunk, n);
-    int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.geoms, S.ncol, i0 + threadIdx.x) : 0;
+    int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.cbase, S.ncol, i0 + threadIdx.x) : 0;
     for (int base = i0; base < i1; base += blockDim.x) {  // same trip count for every thread
         const int i = base + threadIdx.x;
         unsigned lo0 = kKeyPosInf, lo1 = kKeyPosInf, lo2 = kKeyPosInf;
         unsigned hi0 = kKeyNegInf, hi1 = kKeyNegInf, hi2 = kKeyNegInf;
         if (i < i1) {
-            while (colony + 1 < S.ncol && __ldg(&S.geoms[colony].slot_end) <= i) ++colony;
+            while (colony + 1 < S.ncol && __ldg(&S.cbase[colony + 1]) <= i) ++colony;
             const DevGeom &G = S.geoms[colony];
             const float4 me = rel_a[i];
             const int4 rec = __ldg(&S.lrec[i]);
