@@ -218,14 +218,13 @@ __global__ void k_list_canon(const DevState S, int a)
 // of the sorted copies.  f(u, dxs, dys, dzs): sorted position and the bin
 // shift of the neighbour relative to (bx, by, izi); the slot's own sorted
 // position self_t is skipped.  (One loop per column over its three z cells
-// keeps the lanes of a warp together better than a loop per cell.)
+// keeps the lanes of a warp together better than a loop per cell; a
+// candidate's z bin follows from the cell boundaries inside the range.)
 template <class F>
 __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G, int self_t, int bx, int by, int izi,
                                             F &&f)
 {
-    constexpr int B = kListBins;
     const int *__restrict__ cs = S.cellstart;
-    const int *__restrict__ siz = S.siz[B];
     const int nz = G.n[2];
     const int z0 = max(izi - 1, 1), z1 = min(izi + 1, nz);
     for (int dxs = -1; dxs <= 1; ++dxs) {
@@ -242,9 +241,12 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
             }
             const int cb = G.cell_base + ((sx - 1) * G.n[1] + (sy - 1)) * nz;
             const int hi = __ldg(&cs[cb + z1]);
+            // z bin of a candidate from the cell boundaries inside the range
+            const int m1 = __ldg(&cs[cb + z0]), m2 = (z1 > z0) ? __ldg(&cs[cb + z0 + 1]) : hi;
+            const int dz0 = z0 - izi;
             for (int u = __ldg(&cs[cb + z0 - 1]); u < hi; ++u) {
                 if (u == self_t) continue;
-                f(u, dxs, dys, __ldg(&siz[u]) - izi);
+                f(u, dxs, dys, dz0 + (u >= m1) + (u >= m2));
             }
         }
     }
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
             const float4 q = __ldg(&S.srel[B][u]);
             const float ex = (me.x - q.x) - (float)dxs * dxb;
             const float ey = (me.y - q.y) - (float)dys * dyb;
-            const float ez = (me.z - q.z) - (float)dzs * dzb;
+            const float ez = (me.z - q.z) - (dzs == 0 ? 0.0f : (dzs > 0 ? dzb : -dzb));
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
             const float lim = (me.w + q.w) + lim0;
             if (!(r2f <= lim * lim)) return;
