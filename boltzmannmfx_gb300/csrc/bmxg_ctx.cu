@@ -24,11 +24,13 @@ struct GraphKey {
     double dt;
     int precision;
     int parity;
+    int single;  // -1: kResyncEvery steps; 0 / 1: one step without / with the FP32F re-sync
     bool operator<(const GraphKey &o) const
     {
         if (dt != o.dt) return dt < o.dt;
         if (precision != o.precision) return precision < o.precision;
-        return parity < o.parity;
+        if (parity != o.parity) return parity < o.parity;
+        return single < o.single;
     }
 };
 
@@ -948,9 +950,9 @@ int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
     return BMXG_OK;
 }
 
-int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec_t *out)
+int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec_t *out, int single = -1)
 {
-    GraphKey key{dt, precision, parity};
+    GraphKey key{dt, precision, parity, single};
     auto it = ctx->graphs.find(key);
     if (it != ctx->graphs.end()) {
         *out = it->second;
@@ -963,7 +965,11 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc2 = BMXG_OK;
     ctx->capturing = true;
-    for (int s = 0; s < kResyncEvery && !rc2; ++s) rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == kResyncEvery - 1);
+    if (single >= 0)
+        rc2 = enqueue_step(ctx, dt, precision, parity, single);
+    else
+        for (int s = 0; s < kResyncEvery && !rc2; ++s)
+            rc2 = enqueue_step(ctx, dt, precision, parity ^ (s & 1), s == kResyncEvery - 1);
     ctx->capturing = false;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc2) {
@@ -1016,12 +1022,20 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int32_t left = nsteps;
     ctx->kev_used = 0;
-    auto eager = [&]() -> int {  // one step outside a graph, on the re-sync schedule
+    auto eager = [&]() -> int {  // one step on the re-sync schedule
         // re-sync on the last step of each kResyncEvery (not right after a load,
         // whose offsets are exact)
-        int rc = enqueue_step(ctx, subdt, precision, ctx->parity,
-                              ctx->step_count % kResyncEvery == kResyncEvery - 1);
-        if (rc) return rc;
+        const int resync = (ctx->step_count % kResyncEvery == kResyncEvery - 1) ? 1 : 0;
+        if (ctx->profiling) {  // launched one by one, with events around the force kernel
+            int rc = enqueue_step(ctx, subdt, precision, ctx->parity, resync);
+            if (rc) return rc;
+        } else {  // a captured one-step graph: one launch instead of the step's kernels and copies
+            cudaGraphExec_t g1 = nullptr;
+            int rc = get_graph(ctx, subdt, precision, ctx->parity, &g1, resync);
+            if (rc) return rc;
+            CK(cudaGraphLaunch(g1, ctx->stream));
+            ctx->launches += ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity, resync}];
+        }
         ctx->parity ^= 1;
         ++ctx->step_count;
         --left;
@@ -1039,7 +1053,7 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
         // the other parity's graph too, so that a later call needs no capture
         if (!rc) rc = get_graph(ctx, subdt, precision, ctx->parity ^ 1, &g_other);
         if (rc) return rc;
-        const int per = ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity}];
+        const int per = ctx->graph_kernels[GraphKey{subdt, precision, ctx->parity, -1}];
         while (left >= kResyncEvery) {
             CK(cudaGraphLaunch(g, ctx->stream));
             ctx->launches += per;
