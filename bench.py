@@ -59,6 +59,19 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(ms, device):
+    """The slowest rank's time: every rank runs the same replica workload and
+    the whole job is done when the last one is (no-op on one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
 def workload(name):
     from boltzmannmfx_gb300 import configs
     return {"colonies": configs.colonies, "sphere_fp32": configs.sphere_fp32,
@@ -316,11 +329,7 @@ def run_ours(args):
     launches = s1["n_kernel_launches"] - l0
     rebins = s1["n_rebins"] - r0  # bin-order rebuilds: one per step, or one per list build
     list_mode = kind == "sphere" and prec == BMXG_FP32F and rebins < args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    ms = max_over_ranks(ms, "cuda")
     value = N * world * args.steps / (ms / 1e3)
 
     # roofline: the force kernel timed per launch (profiling mode, eager
