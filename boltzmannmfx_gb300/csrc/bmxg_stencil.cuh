@@ -27,7 +27,8 @@ __device__ __forceinline__ bool image_in_row(const DevState &S, const DevGeom &G
 // Visit slot i's neighbour candidates in the order of the reference's
 // neighbour list: stencil bins x outermost, then y, then z, ascending
 // original index within a bin (AMReX NeighborList over the 27 bins around
-// the particle's bin, periodic images from the one-cell halo).
+// the particle's bin, periodic images from the one-cell halo).  Each column is
+// entered by binary search at its first entry of z bin izi - 1.
 // f(j, dxs, dys, dzs, sx, sy): dxs/dys/dzs = neighbour bin minus own bin,
 // sx/sy = image shift in units of the domain length.
 template <class F>
@@ -42,7 +43,13 @@ __device__ __forceinline__ void visit_stencil(const DevState &S, const DevGeom &
             int cc, sx, sy;
             if (!stencil_row(G, ii, jj, cc, sx, sy)) continue;
             const int t1 = __ldg(&cs[cc + 1]);
-            for (int t = __ldg(&cs[cc]); t < t1; ++t) {
+            int t0 = __ldg(&cs[cc]);
+            for (int hi2 = t1; t0 < hi2;) {  // first entry of z bin >= izi - 1
+                const int mid = (t0 + hi2) >> 1;
+                if (__ldg(&izs[__ldg(&perm[mid])]) < izi - 1) t0 = mid + 1;
+                else hi2 = mid;
+            }
+            for (int t = t0; t < t1; ++t) {
                 const int j = __ldg(&perm[t]);
                 const int dzs = __ldg(&izs[j]) - izi;
                 if (dzs > 1) break;  // a column is sorted by z-bin: the rest is out of reach
