@@ -552,9 +552,13 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     S.cbase = ctx->d_cbase;
     S.cnt = ctx->d_cnt;
     cudaStream_t st = ctx->stream;
-    CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol, cudaMemcpyHostToDevice, st));
-    ctx->h_cbase.assign(off.begin(), off.end());
-    CK(cudaMemcpyAsync(ctx->d_cbase, ctx->h_cbase.data(), sizeof(int) * (ctx->ncol + 1), cudaMemcpyHostToDevice, st));
+    if (!reuse) {  // same colonies as the loaded state: the device copies are current
+        CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol, cudaMemcpyHostToDevice,
+                           st));
+        ctx->h_cbase.assign(off.begin(), off.end());
+        CK(cudaMemcpyAsync(ctx->d_cbase, ctx->h_cbase.data(), sizeof(int) * (ctx->ncol + 1), cudaMemcpyHostToDevice,
+                           st));
+    }
     CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
     CK(cudaMemsetAsync(S.colcnt, 0, sizeof(int) * std::max<int64_t>(ncols, 1), st));
     if (n == 0) {
@@ -673,9 +677,12 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     // overlaps the scatter of the next.
     JoinIo join{nullptr};
     int used = 0;
+    const bool pipe = host;  // (copies on `st` instead measured slower at every size)
     if (host) {
         int rc0 = ensure_io(ctx, (size_t)n * 48 + 256);
         if (rc0) return rc0;
+    }
+    if (pipe) {
         CK(cudaEventRecord(ctx->io_ev[0], st));
         CK(cudaStreamWaitEvent(st1, ctx->io_ev[0], 0));
         join.s = st1;
@@ -686,7 +693,7 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     auto begin = [&](void *dst) -> void * {
         if (!host) return dst;
         const int h = used & 1;
-        if (used >= 2) {  // the half's previous copy-out is done
+        if (pipe && used >= 2) {  // the half's previous copy-out is done
             const cudaError_t e = cudaStreamWaitEvent(st, ctx->io_ev[4 + h], 0);
             if (e != cudaSuccess) wait_err = e;
         }
@@ -759,7 +766,7 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
             if (f) CK(cudaMemsetAsync(f, 0, sizeof(int32_t) * n, st));
     }
     CK(cudaStreamSynchronize(st));
-    if (host) CK(cudaStreamSynchronize(st1));
+    if (pipe) CK(cudaStreamSynchronize(st1));
     return BMXG_OK;
 }
 
