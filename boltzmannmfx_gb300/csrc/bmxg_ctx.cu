@@ -576,11 +576,11 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     LAUNCH(launch_user_bin(S, src_x, src_y, src_z, S.col[1], S.iz[1], grd, blk, st));
     LAUNCH(launch_scan(S.colcnt, S.colstart[1], (int)ncols, ctx->scan_scratch, st));
     LAUNCH(launch_user_scatter_canon(S, S.col[1], S.iz[1], S.colstart[1], ctx->uperm, grd, blk, st));
-    CK(cudaMemcpyAsync(S.orig, ctx->uperm, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
-    // gather every field into slot order
-    LAUNCH(launch_gather_d(S.x[0], src_x, ctx->uperm, (int)n, grd, blk, st));
-    LAUNCH(launch_gather_d(S.y[0], src_y, ctx->uperm, (int)n, grd, blk, st));
-    LAUNCH(launch_gather_d(S.z[0], src_z, ctx->uperm, (int)n, grd, blk, st));
+    // positions, radii, cell types, bins and offsets into slot order in one
+    // pass (slot s is sorted position s, so the sort's bins are the slots')
+    CK(cudaMemcpyAsync(S.colstart[0], S.colstart[1], sizeof(int) * (ncols + 1), cudaMemcpyDeviceToDevice, st));
+    LAUNCH(launch_load_slots(S, src_x, src_y, src_z, src_r, src_ct, S.col[1], S.iz[1], ctx->uperm, grd, blk, st));
+    // the other fields
     auto up_d = [&](const double *src, double *dst, double fill) -> int {
         if (src) {
             CK(cudaMemcpyAsync(ctx->ud, src, sizeof(double) * n, kind, st));
@@ -604,8 +604,6 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         }
         return BMXG_OK;
     };
-    LAUNCH(launch_gather_d(S.rad, src_r, ctx->uperm, (int)n, grd, blk, st));
-    LAUNCH(launch_gather_i8(S.ctype, src_ct, ctx->uperm, (int)n, grd, blk, st));
     if ((rc = up_d(p->velx, S.vx, 0.0))) return rc;
     if ((rc = up_d(p->vely, S.vy, 0.0))) return rc;
     if ((rc = up_d(p->velz, S.vz, 0.0))) return rc;
@@ -634,13 +632,10 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         if ((rc = up_i(p->site, S.tab[0] + 9 * n, 4, 0))) return rc;
         LAUNCH(launch_trig(S, 0, grd, blk, st));
     }
-    // bins of the slots and the first column lists: the sort above already
-    // has them (slot s is sorted position s)
-    CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
-    CK(cudaMemcpyAsync(S.colstart[0], S.colstart[1], sizeof(int) * (ncols + 1), cudaMemcpyDeviceToDevice, st));
-    LAUNCH(launch_slot_init(S, S.col[1], S.iz[1], ctx->uperm, grd, blk, st));
     CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (ctx->h_cnt->bad_index) return fail(ctx, BMXG_ERR_STATE, "internal: inconsistent bin counts in the load sort");
     ctx->have_state = true;
     ctx->stepped = false;
     ctx->vel32 = false;

@@ -110,9 +110,11 @@ int launch_scatter_canon(const DevState &S, int b, int grid, int block, cudaStre
 int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int block, cudaStream_t st,
                    int ra = -1, const int *gate = nullptr);
 
-// bins, offsets and identity column order of a freshly sorted state (buffer 0)
-int launch_slot_init(const DevState &S, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
-                     cudaStream_t st);
+// positions, radii, cell types, bins, offsets and identity column order of a
+// freshly sorted state (buffer 0), gathered from the caller-order arrays
+int launch_load_slots(const DevState &S, const double *ux, const double *uy, const double *uz, const double *ur,
+                      const int *uct, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
+                      cudaStream_t st);
 // state checks before a load: out[4] = {bad cell type, any FUNGI, largest radius bits, NaN radius}
 int launch_check_state(const int *ct, const double *r, int n, unsigned long long *out, int grid, int block,
                        cudaStream_t st);

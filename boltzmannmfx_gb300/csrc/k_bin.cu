@@ -306,22 +306,32 @@ __global__ void k_check_state(const int *__restrict__ ct, const double *__restri
     }
 }
 
-// Slot s of a freshly sorted state holds caller particle uperm[s]: its bins
-// are the caller-order bins, its column order is the sort's (perm = identity,
-// colstart = the sort's offsets, copied by the caller); offsets and counters
-// as rebin_slot computes them, without computing the bins again.
-__global__ void k_slot_init(const DevState S, const int *ucol, const int *uiz, const int *uperm)
+// Slot s of a freshly sorted state holds caller particle uperm[s]: its
+// position, radius and cell type are gathered from the caller-order arrays,
+// its bins are the caller-order bins of the sort, its column order is the
+// sort's (perm = identity, colstart = the sort's offsets, copied by the
+// caller), and its offsets and counters are place_slot's.
+__global__ void k_load_slots(const DevState S, const double *ux, const double *uy, const double *uz,
+                             const double *ur, const int *uct, const int *ucol, const int *uiz, const int *uperm)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S.n; s += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, s);
         const int u = uperm[s];
+        const double x = ux[u], y = uy[u], z = uz[u], r = ur[u];
+        S.x[0][s] = x;
+        S.y[0][s] = y;
+        S.z[0][s] = z;
+        S.rad[s] = r;
+        S.ctype[s] = (int8_t)uct[u];
+        S.orig[s] = u;
         int bx, by;
         col_to_bxy(G, ucol[u], bx, by);
-        place_slot(S, G, s, S.x[0][s], S.y[0][s], S.z[0][s], S.rad[s], 0, 0, bx, by, uiz[u], true, false);
+        const int bz = uiz[u];
+        place_slot(S, G, s, x, y, z, r, 0, 0, bx, by, bz, true, false);
         S.perm[0][s] = s;
         if (S.srel[0]) {
             S.srel[0][s] = S.rel[0][s];
-            S.siz[0][s] = uiz[u];
+            S.siz[0][s] = bz;
             S.rank[0][s] = s;
         }
     }
@@ -329,10 +339,11 @@ __global__ void k_slot_init(const DevState S, const int *ucol, const int *uiz, c
 
 }  // namespace
 
-int launch_slot_init(const DevState &S, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
-                     cudaStream_t st)
+int launch_load_slots(const DevState &S, const double *ux, const double *uy, const double *uz, const double *ur,
+                      const int *uct, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
+                      cudaStream_t st)
 {
-    k_slot_init<<<grid, block, 0, st>>>(S, ucol, uiz, uperm);
+    k_load_slots<<<grid, block, 0, st>>>(S, ux, uy, uz, ur, uct, ucol, uiz, uperm);
     return 1;
 }
 
