@@ -199,16 +199,24 @@ __device__ __forceinline__ double wall_law(double z, double rS, const DevParams 
 }
 
 // Exact float -> double conversion with integer operations (GB300's FP64
-// pipe is the scarce resource here).  Subnormal floats flush to zero.
+// pipe is the scarce resource here), on the two 32-bit words: for a normal
+// float the high word is the sign, then exponent and mantissa shifted down by
+// three with the exponent rebased by 1023 - 127, and the low word the last
+// three mantissa bits.  Subnormal floats flush to a signed zero; infinities
+// and NaNs keep their payload.
 __device__ __forceinline__ double f2d_int(float f)
 {
     const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
-    if (e == 0u) return __longlong_as_double((long long)s);
-    const unsigned long long ee = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);  // 1023 - 127
-    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
-    return __longlong_as_double((long long)(s | (ee << 52) | m));
+    const unsigned sgn = u & 0x80000000u, a = u & 0x7fffffffu;
+    unsigned hi = sgn | ((a >> 3) + 0x38000000u);
+    unsigned lo = u << 29;
+    if (a < 0x00800000u) {
+        hi = sgn;
+        lo = 0u;
+    } else if (a >= 0x7f800000u) {
+        hi = sgn | 0x7ff00000u | ((a & 0x7fffffu) >> 3);
+    }
+    return __hiloint2double((int)hi, (int)lo);
 }
 
 // growth-surface cubic law in FP32 (bmx_cell_interaction_K.H:1019-1030)
