@@ -126,7 +126,6 @@ int launch_user_scatter_canon(const DevState &S, const int *ucol, const int *uiz
                                int *uperm, int grid, int block, cudaStream_t st);
 int launch_gather_d(double *dst, const double *src, const int *perm, int n, int grid, int block, cudaStream_t st);
 int launch_gather_i(int *dst, const int *src, const int *perm, int n, int planes, int grid, int block, cudaStream_t st);
-int launch_gather_i8(int8_t *dst, const int *src, const int *perm, int n, int grid, int block, cudaStream_t st);
 int launch_scatter_d(double *dst, const double *src, const int *orig, int n, int grid, int block, cudaStream_t st);
 int launch_scatter_f2d(double *dst, const float *src, const int *orig, int n, int grid, int block,
                        cudaStream_t st);

@@ -211,12 +211,6 @@ __global__ void k_gather_i(int *dst, const int *src, const int *perm, int n, int
     }
 }
 
-__global__ void k_gather_i8(int8_t *dst, const int *src, const int *perm, int n)
-{
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
-        dst[s] = (int8_t)src[perm[s]];
-}
-
 __global__ void k_scatter_d(double *dst, const double *src, const int *orig, int n)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
@@ -418,13 +412,6 @@ int launch_gather_i(int *dst, const int *src, const int *perm, int n, int planes
                      cudaStream_t st)
 {
     k_gather_i<<<grid, block, 0, st>>>(dst, src, perm, n, planes);
-    return 1;
-}
-
-int launch_gather_i8(int8_t *dst, const int *src, const int *perm, int n, int grid, int block,
-                      cudaStream_t st)
-{
-    k_gather_i8<<<grid, block, 0, st>>>(dst, src, perm, n);
     return 1;
 }
 
