@@ -199,3 +199,49 @@ def test_fp32f_multistep_bins_stay_exact(gpu_lib, oracle_lib):
     v32 = np.stack([A["velx"], A["vely"], A["velz"]])
     v64 = np.stack([B["velx"], B["vely"], B["velz"]])
     assert relerr(v32, v64) <= 1e-4
+
+
+def test_full_size_colonies(gpu_lib, oracle_lib):
+    """The benchmark's 256-colony workload at full size (2 731 333 spheres):
+    one FP64 step bit-exact against the oracle; the FP32F force error of a list
+    step within 1e-5 of the FP64 step's; 24 FP32F list steps against 24 per-step
+    FP32F steps within 1e-4 in the displacements; and after the list steps the
+    exported pair list equals that of a fresh exact binning of the positions."""
+    import os
+    w = configs.colonies()
+    P = w.particles
+    A = gpu_ctx(w.params, w.geoms, P, w.offsets)
+    A.step(w.dt, 1, BMXG_FP64)
+    Q64 = readback(A, P)
+    R = P.copy()
+    oracle_lib.evolve(w.params, w.geoms, w.offsets, R, w.dt, 1, nthreads=os.cpu_count() or 1)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(Q64[k], R[k]), k
+    # a list step (build + step) and an FP64 step on the same positions
+    A.set_state(P, w.offsets)
+    A.step(w.dt, 1, BMXG_FP64)
+    A.step(w.dt, 1, BMXG_FP32F)
+    assert A.stats()["n_rebins"] == 2   # the FP64 step's binning and one list build
+    C = gpu_ctx(w.params, w.geoms, P, w.offsets)
+    C.step(w.dt, 2, BMXG_FP64)
+    va = np.stack([readback(A, P)[k] for k in ("velx", "vely", "velz")])
+    vc = np.stack([readback(C, P)[k] for k in ("velx", "vely", "velz")])
+    assert relerr(va, vc) <= TOL32
+    # list steps against per-step FP32F steps
+    A.set_state(P, w.offsets)
+    A.step(w.dt, 24, BMXG_FP32F)
+    D = Context(w.params, w.geoms)
+    D.set_list_mode(0)
+    D.set_state(P, w.offsets)
+    D.step(w.dt, 24, BMXG_FP32F)
+    QA, QD = readback(A, P), readback(D, P)
+    assert A.stats()["n_rebins"] < 24 and D.stats()["n_rebins"] == 24
+    L = 0.128
+    for k in ("x", "y"):
+        da = QA[k] - P[k] - L * np.round((QA[k] - P[k]) / L)
+        dd = QD[k] - P[k] - L * np.round((QD[k] - P[k]) / L)
+        assert relerr(da, dd) <= 1e-4, k
+    assert relerr(QA["z"] - P["z"], QD["z"] - P["z"]) <= 1e-4
+    # the pair list after list steps is the exact binning's
+    E = gpu_ctx(w.params, w.geoms, QA, w.offsets)
+    assert same_pairs(A.pairs(), E.pairs())
