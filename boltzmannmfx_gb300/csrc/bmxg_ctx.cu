@@ -294,6 +294,14 @@ void build_geoms(bmxg_ctx *ctx)
             G.dxf[d] = (float)G.dx[d];
             G.plof[d] = (float)G.plo[d];
             G.dxif[d] = (float)G.dxi[d];
+            G.phif[d] = (float)G.phi[d];
+            // corners as the device computes them: a product, then a sum, each
+            // rounded (volatile keeps the host compiler from fusing them)
+            G.ncorner[d] = std::min(G.n[d], kCornerTable);
+            for (int bi = 1; bi <= G.ncorner[d]; ++bi) {
+                volatile double t = (double)(bi - 1) * G.dx[d];
+                G.corner[d][bi - 1] = G.plo[d] + t;
+            }
             G.per[d] = g.is_periodic[d] ? 1 : 0;
             diag2 += 4.0 * G.dx[d] * G.dx[d];
         }

@@ -29,6 +29,7 @@ constexpr int BMXG_FP32F_FORM = 1;              // BMXG_FP32F of bmxg.h
 constexpr int kYeast = 0, kFungi = 1;           // cellType (src/chemistry/bmx_chem.H:120-126)
 constexpr int kTip = 0, kSecond1 = 1, kSecond2 = 2, kInterior = 3;  // siteLocation (bmx_chem.H:128-136)
 constexpr int kWallTable = 66;                  // z-bins with a precomputed wall height (grown box)
+constexpr int kCornerTable = 128;               // bins per axis with a precomputed FP64 corner
 constexpr int kResyncEvery = 8;                 // FP32F: exact FP64 re-binning of every slot each 8th step
 
 // Geometry of one colony (an AMReX level geometry) plus its place in the
@@ -37,6 +38,9 @@ struct DevGeom {
     double plo[3], phi[3], len[3], dx[3], dxi[3];
     float dxf[3];
     float plof[3], dxif[3];  // plo and dxi rounded to FP32 (bin_of_fast; 0: not set, FP64 binning)
+    float phif[3];           // phi rounded to FP32 (0 with plof: not set)
+    int ncorner[3];          // entries of corner (0: not set)
+    double corner[3][kCornerTable];  // plo + (b - 1) dx of bin b, rounded as the device formula
     int n[3];
     int per[3];
     int col_base;       // first global column of this colony
@@ -114,6 +118,25 @@ __device__ __forceinline__ int bin_of_fast(double x, double plo, double dxi, flo
     const float f0 = floorf(__fsub_rn(v, e)), f1 = floorf(__fadd_rn(v, e));
     if (f0 == f1 && dxif > 0.0f && fabsf(f0) < 1.0e7f) return min(max((int)f0, lo_c), hi_c);
     return bin_of(x, plo, dxi, lo_c, hi_c);
+}
+
+// Round-to-nearest double -> float from the bits (no FP64 instruction) where
+// the result is a normal float, the FP32 conversion otherwise; equal to it.
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e < 897u || e > 1150u) return (float)x;
+    const unsigned m23 = (unsigned)(b >> 29) & 0x7fffffu;
+    const unsigned rem = (unsigned)b & 0x1fffffffu;
+    const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) ? 1u : 0u;
+    return __uint_as_float((((unsigned)(b >> 32)) & 0x80000000u) + ((e - 896u) << 23) + m23 + up);
+}
+
+// x is neither infinite nor NaN (bit test)
+__device__ __forceinline__ bool finite_bits(double x)
+{
+    return ((((unsigned long long)__double_as_longlong(x)) >> 52) & 0x7ffull) != 0x7ffull;
 }
 
 // AMReX enforcePeriodic restated: shift by the domain length until inside,

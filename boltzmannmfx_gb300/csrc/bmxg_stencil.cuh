@@ -148,13 +148,25 @@ __device__ __forceinline__ void place_slot(const DevState &S, const DevGeom &G, 
     const int c = column_of(G, bx, by);
     S.col[bb][i] = c;
     S.iz[bb][i] = bz;
-    const double cx = G.plo[0] + (double)(bx - 1) * G.dx[0];
-    const double cy = G.plo[1] + (double)(by - 1) * G.dx[1];
-    const double cz = G.plo[2] + (double)(bz - 1) * G.dx[2];
-    S.rel[rb][i] = make_float4((float)(x - cx), (float)(y - cy), (float)(z - cz), (float)r);
+    // bin corners from the geometry's table (the same FP64 formula, evaluated
+    // once on the host), the conversions and tests from the bits: FP64
+    // arithmetic here is the three differences (GB300 issues FP64 at a small
+    // fraction of the FP32 rate)
+    auto corner = [&](int d, int bin) {
+        return (bin >= 1 && bin <= G.ncorner[d]) ? G.corner[d][bin - 1] : G.plo[d] + (double)(bin - 1) * G.dx[d];
+    };
+    const double cx = corner(0, bx), cy = corner(1, by), cz = corner(2, bz);
+    S.rel[rb][i] = make_float4(d2f_rn(x - cx), d2f_rn(y - cy), d2f_rn(z - cz), d2f_rn(r));
     if (count_col) atomicAdd(&S.colcnt[c], 1);
-    if (count_domain && !(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
-    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicAdd(&S.cnt->nonfinite, 1ULL);
+    if (count_domain) {
+        // inside for certain from the FP32 values (truncated z within 2^-21 of the
+        // magnitudes), else the FP64 test
+        const float zf = d2f_trunc(z);
+        const float m = 4.8e-7f * (fabsf(zf) + fabsf(G.plof[2]) + fabsf(G.phif[2]));
+        const bool sure = G.phif[2] > G.plof[2] && zf - m > G.plof[2] && zf + m < G.phif[2];
+        if (!sure && !(z >= G.plo[2] && z < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+    }
+    if (!finite_bits(x) || !finite_bits(y) || !finite_bits(z)) atomicAdd(&S.cnt->nonfinite, 1ULL);
     if (G.per[0] && (bx == 1 || bx == G.n[0])) {
         const int sx = (bx == 1) ? 1 : -1;
         const int gb = bin_of(x + (double)sx * G.len[0], G.plo[0], G.dxi[0], 0, G.n[0] + 1);

@@ -53,6 +53,7 @@ template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)
 {
     const int b = a ^ 1;
+    const float bwf = (float)P.bw;  // once per thread: a conversion is an FP64-pipe instruction
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, i);
         int bx, by;
@@ -70,7 +71,7 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
             const float ey = (me.y - q.y) - (float)dys * dyb;
             const float ez = (me.z - q.z) - (float)dzs * dzb;
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), (float)P.bw), slack);
+            const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), bwf), slack);
             if (r2f > __fmul_rn(lim, lim)) return;
             const int j = slot();
             const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
@@ -110,12 +111,14 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
 }
 
 template <bool SORTED>
-__global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, double dt, int a,
+__global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, float dtf, int a,
                                                   int resync)
 {
     const int b = a ^ 1;
-    const float bwf = (float)P.bw, kf = (float)P.k, dtf = (float)dt;
-    const float zkf = (float)P.z_k, zbwf = (float)P.z_bw, zgf = (float)P.z_g;
+    // the FP32 roundings come from the host (a conversion is an FP64-pipe
+    // instruction, and threads without a slot would issue them too)
+    const float bwf = P.bw32, kf = P.k32;
+    const float zkf = P.z_k32, zbwf = P.z_bw32, zgf = P.z_g32;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, i);
         const int col = S.col[a][i];
@@ -202,8 +205,8 @@ int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, 
         if (sorted) k_sphere64<true><<<grid, block, 0, st>>>(S, P, dt, a);
         else k_sphere64<false><<<grid, block, 0, st>>>(S, P, dt, a);
     } else {
-        if (sorted) k_sphere32<true><<<grid, block, 0, st>>>(S, P, dt, a, resync);
-        else k_sphere32<false><<<grid, block, 0, st>>>(S, P, dt, a, resync);
+        if (sorted) k_sphere32<true><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
+        else k_sphere32<false><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
     }
     return 1;
 }
