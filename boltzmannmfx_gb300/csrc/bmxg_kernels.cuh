@@ -8,6 +8,16 @@
 
 namespace bmxg {
 
+__host__ __device__ __forceinline__ double4_32a make_trig(double ct, double st, double cp, double sp)
+{
+    double4_32a t;
+    t.x = ct;
+    t.y = st;
+    t.z = cp;
+    t.w = sp;
+    return t;
+}
+
 // Control block of the FP32F neighbour list with a skin (k_list.cu).  The
 // list stays valid while no pair's separation has changed by the skin since
 // it was built; acc bounds that change from above.
@@ -74,7 +84,7 @@ struct DevState {
     int has_rods;
     double *clen, *area, *bscale;
     double *theta[2], *phi[2];
-    double4 *trig[2];  // (cos theta, sin theta, cos phi, sin phi)
+    double4_32a *trig[2];  // (cos theta, sin theta, cos phi, sin phi)
     int *id, *cpu, *fuse_tip;
     int *tab[2];       // 13 planes: n_bnds, ids[4], cpus[4], sites[4]
     int *position, *fix_site, *fflag, *sflag, *nflag;

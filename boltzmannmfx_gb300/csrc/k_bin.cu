@@ -235,7 +235,7 @@ __global__ void k_trig(const DevState S, int b)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const double th = S.theta[b][i], ph = S.phi[b][i];
-        S.trig[b][i] = make_double4(cos(th), sin(th), cos(ph), sin(ph));
+        S.trig[b][i] = make_trig(cos(th), sin(th), cos(ph), sin(ph));
     }
 }
 

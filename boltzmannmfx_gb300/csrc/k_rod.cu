@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
             acc[2] += wall_law(zi, ri, P);
         } else if (ti == kFungi) {
             const double Li = S.clen[i];
-            const double4 tri = S.trig[a][i];  // (ct, st, cp, sp)
+            const double4_32a tri = S.trig[a][i];  // (ct, st, cp, sp)
             const double ni[3] = {tri.y * tri.z, tri.y * tri.w, tri.x};
             const int iid = S.id[i], icpu = S.cpu[i];
             const int itip = S.fuse_tip[i];
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                         if ((itip > 0 && itip == si) || (jtip > 0 && jtip == sj)) kb = bsi * S.bscale[j] * kb;
                     }
                 }
-                const double4 trj = S.trig[a][j];
+                const double4_32a trj = S.trig[a][j];
                 const double rS = ri + S.rad[j];
                 const double rA = rS + P.bw;
                 double f1[3], f2[3];
@@ -454,7 +454,7 @@ __global__ void k_rod_update(const DevState S, double dt, int a)
         double ny = S.y[a][i] + dt * v[1];
         const double nz = S.z[a][i] + dt * v[2];
         double th = S.theta[a][i], ph = S.phi[a][i];
-        double4 tr = S.trig[a][i];
+        double4_32a tr = S.trig[a][i];
         if (S.ctype[i] == kFungi) {
             // rotate the axis by |omega| dt (bmx_pc_interaction.cpp:334-431)
             const double ct = tr.x, st = tr.y, cp = tr.z, sp = tr.w;
@@ -491,7 +491,7 @@ __global__ void k_rod_update(const DevState S, double dt, int a)
             if (rho > 0.0) nd[0] /= rho;
             ph = acos(nd[0]);
             if (nd[1] < 0.0) ph = 2.0 * kPi - ph;
-            tr = make_double4(cos(th), sin(th), cos(ph), sin(ph));
+            tr = make_trig(cos(th), sin(th), cos(ph), sin(ph));
         }
         S.theta[b][i] = th;
         S.phi[b][i] = ph;
@@ -525,7 +525,7 @@ __global__ void k_init_bonds(const DevState S, const DevParams P, int a, double 
         col_to_bxy(G, S.col[a][i], bx, by);
         const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
         const double Li = S.clen[i];
-        const double4 tri = S.trig[a][i];
+        const double4_32a tri = S.trig[a][i];
         const double ni[3] = {tri.y * tri.z, tri.y * tri.w, tri.x};
         int nb = S.tab[a][i];
         unsigned long long add = 0, over = 0;
@@ -537,7 +537,7 @@ __global__ void k_init_bonds(const DevState S, const DevParams P, int a, double 
             const double Lj = S.clen[j];
             const double rlm = 1.5 * (Li + Lj) + P.bw;
             if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
-            const double4 trj = S.trig[a][j];
+            const double4_32a trj = S.trig[a][j];
             const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
             double e[4][3];  // i1, i2, j1, j2 with j's centre at the origin
             for (int k = 0; k < 3; ++k) {
