@@ -38,12 +38,6 @@ namespace {
 
 constexpr unsigned kSlotMask = (1u << kNbrShift) - 1u;
 
-// bin shift code (0, 1, 2) -> -width, 0, +width
-__device__ __forceinline__ float shift_of(unsigned c, float w)
-{
-    return (c == 1u) ? 0.0f : ((c == 0u) ? -w : w);
-}
-
 // Order-preserving unsigned key of a float (and back): atomicMin / atomicMax
 // on the keys order the floats.
 __device__ __forceinline__ unsigned fkey(float f)
@@ -365,7 +359,7 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
             if (cnt <= kNbrCap) {
                 auto entry = [&](unsigned e, const float4 q) {
                     const unsigned code = e >> kNbrShift;
-                    pair(q, shift_of(code & 3u, dxb), shift_of((code >> 2) & 3u, dyb), shift_of((code >> 4) & 3u, dzb));
+                    pair(q, (float)((int)(code & 3u) - 1) * dxb, (float)((int)((code >> 2) & 3u) - 1) * dyb, (float)((int)((code >> 4) & 3u) - 1) * dzb);
                 };
                 // the first entries came with the metadata: their gathers go out
                 // together, one round trip for the typical short list
