@@ -45,7 +45,7 @@ struct ListCtl {
 
 constexpr int kNbrCap = 32;          // list entries per slot (more: the slot walks its stencil)
 constexpr int kNbrInline = 3;        // entries held in the slot's list record beside its metadata
-constexpr int kNbrShift = 26;        // entry = slot | (shift code << 26)
+constexpr int kNbrShift = 26;        // entry = slot | (bin shifts << 26)
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
 
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
@@ -93,7 +93,8 @@ struct DevState {
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
     int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry:
-                       // neighbour slot | (dx, dy, dz bin shift + 1) << 26
+                       // neighbour slot | bin shifts dx, dy, dz in -1..1 as signed 2-bit
+                       // fields at bits 26-27, 28-29, 30-31
     int4 *lrec;        // per slot: x = z bin (bits 0-15), edge flags (16-18), list length
                        // (20-27, saturating); y, z, w = the first kNbrInline entries
     int *cellcnt;      // per 3D cell counter, zero between uses

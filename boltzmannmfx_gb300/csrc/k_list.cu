@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(256) k_list_build(const DevState S, const DevP
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
             const float lim = (me.w + q.w) + lim0;
             if (!(r2f <= lim * lim)) return;
-            const unsigned code = (unsigned)(dxs + 1) | ((unsigned)(dys + 1) << 2) | ((unsigned)(dzs + 1) << 4);
+            const unsigned code = (unsigned)(dxs & 3) | ((unsigned)(dys & 3) << 2) | ((unsigned)(dzs & 3) << 4);
             const int e = (int)((unsigned)__ldg(&S.perm[B][u]) | (code << kNbrShift));
             if (c == 0) rec.y = e;
             else if (c == 1) rec.z = e;
@@ -358,8 +358,9 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
             };
             if (cnt <= kNbrCap) {
                 auto entry = [&](unsigned e, const float4 q) {
-                    const unsigned code = e >> kNbrShift;
-                    pair(q, (float)((int)(code & 3u) - 1) * dxb, (float)((int)((code >> 2) & 3u) - 1) * dyb, (float)((int)((code >> 4) & 3u) - 1) * dzb);
+                    // signed 2-bit shifts at bits 26-27, 28-29, 30-31
+                    pair(q, (float)((int)(e << 4) >> 30) * dxb, (float)((int)(e << 2) >> 30) * dyb,
+                         (float)((int)e >> 30) * dzb);
                 };
                 // the first entries came with the metadata: their gathers go out
                 // together, one round trip for the typical short list
