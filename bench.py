@@ -187,6 +187,70 @@ def adjoint_cost(Context, configs, BMXG_FP64, nsteps=200, ckpt=20):
             "adjoint_over_forward": b_ms / f_ms, "adjoint_over_plain_fp64": b_ms / p_ms}
 
 
+def split_cost(n, seed, reps=10, frac=0.05):
+    """YEAST division (bmxg_split_cells_aos) on n device-resident AoS records
+    (BMX's 448-byte particles, about frac of them above max_vol, seeded draws):
+    device time per call with CUDA events around it on torch's stream (each
+    call on a fresh copy of the records; the call includes its host read of the
+    division count), the host-buffer call's wall time, and the oracle on the
+    same records on one host core.  Algorithmic bytes per call: 12 B per record
+    per flag pass (cell_type 4 + vol 8, two passes) + 968 B per division (the
+    mother read 444, her changed fields written 80, the daughter written 444)."""
+    import torch
+    from boltzmannmfx_gb300 import runtime
+    from boltzmannmfx_gb300.abi import BMXG_DEVICE, INT_IDX, REAL_IDX, SplitParams, aos_dtype
+    from oracle import oracle as O
+    sp = SplitParams(max_vol=5.0e-10, overlap=0.2, max_len=0.0035, max_rad=0.00025, brnch_prob=0.0,
+                     num_reals=9, num_ints=0)
+    rng = np.random.default_rng(seed)
+    cap = n + n // 8
+    a = np.zeros(cap, aos_dtype())
+    a["pos"][:n] = rng.uniform(-1.0e-3, 1.0e-3, (n, 3))
+    vol = 5.0e-10 * np.where(rng.random(n) < frac, rng.uniform(1.0001, 1.9, n), rng.uniform(0.4, 1.0, n))
+    r = (3.0 * vol / (4.0 * np.pi)) ** (1.0 / 3.0)
+    a["rdata"][:n, REAL_IDX["vol"]] = vol
+    a["rdata"][:n, REAL_IDX["radius"]] = r
+    a["rdata"][:n, REAL_IDX["area"]] = 4.0 * np.pi * r * r
+    a["id"][:n] = np.arange(1, n + 1)
+    a["idata"][:n, INT_IDX["id"]] = a["id"][:n]
+    pristine = torch.from_numpy(a.view(np.uint8)).cuda()
+    work = torch.empty_like(pristine)
+    st = torch.cuda.current_stream()
+    times = []
+    k = 0
+    for it in range(reps + 3):
+        work.copy_(pristine)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        k = runtime.split_cells_aos(work.data_ptr(), n, sp, seed=it, next_id=n + 1, where=BMXG_DEVICE,
+                                    cap=cap, stream=st.cuda_stream)
+        e1.record(st)
+        e1.synchronize()
+        if it >= 3:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    host_s = []
+    for it in range(3):
+        h = a.copy()
+        t0 = time.perf_counter()
+        runtime.split_cells_aos(h, n, sp, seed=it, next_id=n + 1)
+        host_s.append(time.perf_counter() - t0)
+    h = a.copy()
+    t0 = time.perf_counter()
+    rc, kc = O.split_cells(h, n, sp, seed=0, next_id=n + 1)
+    cpu_s = time.perf_counter() - t0
+    alg = 24 * n + 968 * k
+    peak, _ = measured_peak()
+    return {"call": "bmxg_split_cells_aos (device records)", "records": n, "divisions": k,
+            "ms_per_call": ms, "records_per_s": n / (ms * 1e-3),
+            "alg_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
+            "frac_of_measured_hbm": (alg / (ms * 1e-3) / 1e9) / peak if peak else None,
+            "host_records_ms": 1e3 * float(np.median(host_s)),
+            "cpu_baseline": {"kind": "port", "cores": 1, "ms_per_call": 1e3 * cpu_s,
+                             "records_per_s": n / cpu_s, "rc": rc, "divisions": kc}}
+
+
 def cpu_baseline(w, budget_s=12.0):
     """Oracle (OpenMP over particles, all host threads) on a bounded sample of
     the workload: whole colonies until ~budget_s of CPU work."""
@@ -399,8 +463,10 @@ def run_ours(args):
            "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)"}
 
     adj = None
+    split = None
     if rank == 0 and w.name.startswith("colonies"):
         adj = adjoint_cost(Context, configs, BMXG_FP64)
+        split = split_cost(N, configs.SEED + 2)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -418,7 +484,7 @@ def run_ours(args):
                            "l2": ("L2 flushed between steps" if flush else
                                   f"inputs larger than L2 (state {state_bytes / 2**20:.0f} MiB)")},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "adjoint": adj,
+                "adjoint": adj, "split": split,
                 "step_structure": ({"kind": "FP32F neighbour list with a skin", "list_builds": int(rebins),
                                     "steps": args.steps,
                                     "per_step": "k_list_decide + k_list_step",

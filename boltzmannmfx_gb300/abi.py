@@ -80,6 +80,33 @@ class Stats(C.Structure):
                 ("main_kernel_ms", C.c_double), ("last_step_ms", C.c_double)]
 
 
+class SplitParams(C.Structure):
+    """bmxg_split_params: parameters of the YEAST division step."""
+    _fields_ = [("max_vol", C.c_double), ("overlap", C.c_double), ("max_len", C.c_double),
+                ("max_rad", C.c_double), ("brnch_prob", C.c_double),
+                ("num_reals", C.c_int32), ("num_ints", C.c_int32)]
+
+
+# positions in amrex::Particle's rdata / idata (realIdx, intIdx of
+# src/chemistry/bmx_chem.H:38-118)
+REAL_IDX = dict(radius=0, c_length=1, theta=2, phi=3, area=4, vol=5, velx=6, vely=7, velz=8,
+                wx=9, wy=10, wz=11, fx=12, fy=13, fz=14, dadt=21, dvdt=22, tau_split=23,
+                bond_scale=24, first_data=25)
+INT_IDX = dict(cell_type=5, n_bnds=6, position=19, fuse_flag=20, split_flag=21, new_flag=22,
+               fuse_tip=25, fix_site=32, id=33, cpu=34, first_data=35)
+
+
+def aos_dtype(nreal=34, nint=35):
+    """numpy dtype of amrex::Particle<nreal, nint> in AMReX 22.x, double
+    precision: pos[3], rdata[nreal], id, cpu, idata[nint], padded to 8 bytes
+    (448 bytes for BMX's 34 / 35)."""
+    fields = [("pos", "<f8", 3), ("rdata", "<f8", nreal), ("id", "<i4"), ("cpu", "<i4"),
+              ("idata", "<i4", nint)]
+    if nint % 2:
+        fields.append(("pad", "<i4"))
+    return np.dtype(fields)
+
+
 REAL_FIELDS = ("x", "y", "z", "radius", "c_length", "theta", "phi", "area",
                "bond_scale", "velx", "vely", "velz", "wx", "wy", "wz")
 INT_FIELDS = ("cell_type", "id", "cpu", "n_bnds", "position", "fuse_tip",

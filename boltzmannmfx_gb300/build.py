@@ -15,8 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbmxg.so")
-SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "k_adjoint.cu", "k_noalloc.cu", "k_list.cu", "bmxg_ctx.cu",
-           "bmxg_aos.cpp", "bmxg_io.cpp"]
+SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "k_adjoint.cu", "k_noalloc.cu", "k_list.cu", "k_split.cu",
+           "bmxg_ctx.cu", "bmxg_aos.cpp", "bmxg_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

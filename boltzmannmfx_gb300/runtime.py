@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import Geometry, Params, Particles, ParticlesStruct, Stats
+from .abi import Geometry, Params, Particles, ParticlesStruct, SplitParams, Stats
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbmxg.so")
@@ -27,7 +27,7 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
                "bmxg_particle_exchange", "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk",
                "bmxg_read_checkpoint",
-               "bmxg_io_last_error", "bmxg_autotune")
+               "bmxg_io_last_error", "bmxg_autotune", "bmxg_split_cells_aos")
 
 
 class Ext(C.Structure):
@@ -85,6 +85,9 @@ def load_library(path=None):
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
     L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
         [C.c_double, vp]
+    L.bmxg_split_cells_aos.argtypes = [C.POINTER(SplitParams), vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                       vp, C.c_int64, C.c_uint64, C.c_int64, C.c_int32, C.c_int32,
+                                       C.POINTER(C.c_int64), vp]
     L.bmxg_forward.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
     L.bmxg_backward.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_double)]
@@ -286,3 +289,37 @@ def read_checkpoint(particles_dir, level=-1):
     particles_dir is the checkpoint's `particles` directory."""
     L = load_library()
     return _two_call(L.bmxg_read_checkpoint, os.fsencode(particles_dir), int(level))
+
+
+def split_cells_aos(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, where=abi.BMXG_HOST,
+                    nreal=34, nint=35, cap=None, stream=None):
+    """YEAST division (bmxg_split_cells_aos) on AoS records.
+
+    where=BMXG_HOST: `records` is a numpy array of abi.aos_dtype(nreal, nint)
+    holding n particles and room for the daughters (len(records) = cap), and
+    `draws` a float64 numpy array or None.  where=BMXG_DEVICE: `records` and
+    `draws` are device addresses (ints, e.g. tensor.data_ptr()) and `cap` is
+    required.  Returns the number of divisions; raises BmxgError."""
+    L = load_library()
+    if where == abi.BMXG_HOST:
+        if records.dtype != abi.aos_dtype(nreal, nint):
+            raise ValueError("records must have abi.aos_dtype(nreal, nint)")
+        cap = len(records) if cap is None else cap
+        ptr = records.ctypes.data_as(C.c_void_p)
+        if draws is not None:
+            draws = np.ascontiguousarray(draws, dtype=np.float64)
+            nd, dptr = draws.size, draws.ctypes.data_as(C.c_void_p)
+        else:
+            nd, dptr = 0, None
+    else:
+        if cap is None:
+            raise ValueError("cap is required for device records")
+        ptr = C.c_void_p(int(records))
+        nd, dptr = (0, None) if draws is None else (int(draws[1]), C.c_void_p(int(draws[0])))
+    out = C.c_int64(0)
+    rc = L.bmxg_split_cells_aos(C.byref(sp), ptr, int(n), int(cap), int(nreal), int(nint), dptr, int(nd),
+                                int(seed) & (2**64 - 1), int(next_id), int(my_proc), int(where), C.byref(out),
+                                None if stream is None else C.c_void_p(int(stream)))
+    if rc != abi.BMXG_OK:
+        raise BmxgError(rc, f"split_cells_aos ({out.value} divisions)")
+    return out.value

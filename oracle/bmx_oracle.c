@@ -975,3 +975,124 @@ int orc_particle_exchange(const bmxg_geometry *geom, const bmxg_particles *p, co
     free(inc);
     return BMXG_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* YEAST division (split_particles)                                          */
+/* ------------------------------------------------------------------------ */
+
+/* realIdx / intIdx positions the division touches (bmx_chem.H:38-118) */
+enum { SR_radius = 0, SR_c_length = 1, SR_area = 4, SR_vol = 5, SR_dadt = 21, SR_dvdt = 22,
+       SR_bond_scale = 24, SR_first = 25 };
+enum { SI_cell_type = 5, SI_position = 19, SI_fuse_tip = 25, SI_id = 33, SI_cpu = 34, SI_first = 35 };
+
+/* SplitMix64 (Steele, Lea and Flood, OOPSLA 2014) on the counter (cpu, id, j),
+ * 53 bits to a double in [0, 1): the draws of the library's seeded mode. */
+double orc_split_uniform(uint64_t seed, int32_t id, int32_t cpu, int32_t j)
+{
+    const uint64_t key = ((uint64_t)(uint32_t)cpu << 32) | (uint64_t)(uint32_t)id;
+    uint64_t z = seed + UINT64_C(0x9E3779B97F4A7C15) * (key * 2u + (uint64_t)j + 1u);
+    z = (z ^ (z >> 30)) * UINT64_C(0xBF58476D1CE4E5B9);
+    z = (z ^ (z >> 27)) * UINT64_C(0x94D049BB133111EB);
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53;
+}
+
+/* checkSplit (bmx_chem_K.H:23-69) without its draws: 1 = a YEAST cell with
+ * vol > max_vol; 2 = a FUNGI tip long and wide enough to split, or a segment
+ * behind a tip that may branch (outside the restated part); 0 = neither. */
+static int split_kind(const bmxg_split_params *sp, const double *r, const int *q)
+{
+    if (q[SI_cell_type] == BMXG_YEAST) return r[SR_vol] > sp->max_vol ? 1 : 0;
+    if (q[SI_cell_type] == BMXG_FUNGI) {
+        if (q[SI_position] == BMXG_SITE_TIP)
+            return (r[SR_radius] >= sp->max_rad && r[SR_c_length] >= sp->max_len) ? 2 : 0;
+        if (q[SI_position] == BMXG_SITE_SECOND_1 || q[SI_position] == BMXG_SITE_SECOND_2)
+            return sp->brnch_prob > 0.0 ? 2 : 0;
+    }
+    return 0;
+}
+
+/* Pass 1 counts the dividing cells (the scan's total, bmx_split_particles.cpp:
+ * 44-66); pass 2 walks them in array order, daughter k at record n + k with id
+ * next_id + k (:68-121): copyChildParameters (bmx_chem_K.H:357-370) copies
+ * reals [0, first_data + num_reals) and ints [0, first_data + num_ints);
+ * setNewCell (:383-440) moves mother and daughter apart by (1 - overlap) r / 2
+ * each along n = (sin t cos p, sin t sin p, cos t), cos t = 2 u1 - 1,
+ * p = 2 pi u2, halves the volume, sets radius, area and dadt from it, resets
+ * the daughter's bond_scale and fuse_tip and halves both cells' species
+ * increments first_data + 6..8. */
+int orc_split_cells_aos(const bmxg_split_params *sp, void *particles, int64_t n, int64_t cap,
+                        int32_t nreal, int32_t nint, const double *draws, int64_t ndraws,
+                        uint64_t seed, int64_t next_id, int32_t my_proc, int64_t *num_split)
+{
+    if (!sp || !num_split || n < 0 || cap < n) return BMXG_ERR_ARG;
+    *num_split = 0;
+    if (nreal < SR_first + 9 || nint < SI_first) return BMXG_ERR_ARG;
+    if (sp->num_reals < 0 || sp->num_ints < 0 || SR_first + sp->num_reals > nreal ||
+        SI_first + sp->num_ints > nint)
+        return BMXG_ERR_ARG;
+    if (n == 0) return BMXG_OK;
+    if (!particles) return BMXG_ERR_ARG;
+    const size_t off_r = 3 * sizeof(double);
+    const size_t off_id = off_r + (size_t)nreal * sizeof(double);
+    const size_t off_i = off_id + 2 * sizeof(int);
+    const size_t stride = (off_i + (size_t)nint * sizeof(int) + 7) / 8 * 8;
+    unsigned char *base = (unsigned char *)particles;
+#define REC(i) (base + (size_t)(i) * stride)
+    int64_t total = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const int kind = split_kind(sp, (const double *)(REC(i) + off_r), (const int *)(REC(i) + off_i));
+        if (kind == 2) return BMXG_ERR_UNSUPPORTED;
+        total += kind;
+    }
+    *num_split = total;
+    if (total == 0) return BMXG_OK;
+    if (n + total > cap) return BMXG_ERR_CAPACITY;
+    if (draws && ndraws < 2 * total) return BMXG_ERR_ARG;
+    const int nreals = SR_first + sp->num_reals, nints = SI_first + sp->num_ints;
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        unsigned char *m = REC(i), *d = REC(n + k);
+        double *mp = (double *)m, *dp = (double *)d;
+        double *mr = (double *)(m + off_r), *dr = (double *)(d + off_r);
+        int *mi = (int *)(m + off_i), *di = (int *)(d + off_i);
+        const int *mid = (const int *)(m + off_id);
+        int *did = (int *)(d + off_id);
+        if (split_kind(sp, mr, mi) != 1) continue;
+        for (int j = 0; j < nreals; ++j) dr[j] = mr[j];
+        for (int j = 0; j < nints; ++j) di[j] = mi[j];
+        const double u1 = draws ? draws[2 * k] : orc_split_uniform(seed, mid[0], mid[1], 0);
+        const double u2 = draws ? draws[2 * k + 1] : orc_split_uniform(seed, mid[0], mid[1], 1);
+        const double x = mp[0], y = mp[1], z = mp[2];
+        double radius = dr[SR_radius];
+        const double theta = acos(2.0 * u1 - 1.0);
+        const double phi = 2.0 * ORC_PI * u2;
+        const double nx = sin(theta) * cos(phi), ny = sin(theta) * sin(phi), nz = cos(theta);
+        const double half = (1.0 - sp->overlap) * 0.5;
+        dp[0] = x + half * nx * radius;
+        dp[1] = y + half * ny * radius;
+        dp[2] = z + half * nz * radius;
+        mp[0] = x - half * nx * radius;
+        mp[1] = y - half * ny * radius;
+        mp[2] = z - half * nz * radius;
+        const double volume = mr[SR_vol] / 2.0;
+        radius = pow(3.0 * volume / (4.0 * ORC_PI), 1.0 / 3.0);
+        const double area = 4.0 * ORC_PI * radius * radius;
+        const double dadt = 2.0 * mr[SR_dvdt] / radius;
+        mr[SR_vol] = dr[SR_vol] = volume;
+        mr[SR_area] = dr[SR_area] = area;
+        mr[SR_dadt] = dr[SR_dadt] = dadt;
+        mr[SR_radius] = dr[SR_radius] = radius;
+        dr[SR_bond_scale] = 1.0;
+        di[SI_fuse_tip] = 0;
+        for (int j = 6; j < 9; ++j) {
+            mr[SR_first + j] = 0.5 * mr[SR_first + j];
+            dr[SR_first + j] = 0.5 * dr[SR_first + j];
+        }
+        did[0] = di[SI_id] = (int)(next_id + k);
+        did[1] = di[SI_cpu] = my_proc;
+        ++k;
+    }
+#undef REC
+    return BMXG_OK;
+}

@@ -12,7 +12,7 @@ import subprocess
 import numpy as np
 
 from boltzmannmfx_gb300.abi import (BMXG_ERR_CAPACITY, BMXG_OK, Geometry, Params,
-                                    Particles, ParticlesStruct)
+                                    Particles, ParticlesStruct, SplitParams)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -63,6 +63,11 @@ def lib():
         L.orc_min_distance.restype = None
         L.orc_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double, _i64, _i64]
         L.orc_particle_exchange.argtypes = [_G, _S, _i64, _i32, _d, _d, C.c_double, _d]
+        L.orc_split_cells_aos.argtypes = [C.POINTER(SplitParams), C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
+                                          C.c_int32, C.c_void_p, C.c_int64, C.c_uint64, C.c_int64, C.c_int32,
+                                          _i64]
+        L.orc_split_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_split_uniform.restype = C.c_double
         _lib = L
     return _lib
 
@@ -90,6 +95,8 @@ def reflib():
         L.ref_surface_force.restype = None
         L.ref_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double]
         L.ref_particle_exchange.argtypes = [_S, _i64, _i32, _i8, _G, _d, _d, C.c_double, _d]
+        L.ref_split_cells_aos.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(SplitParams), C.c_double,
+                                          C.c_double, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, _i64, _i64]
         _ref = L
     return _ref
 
@@ -289,3 +296,32 @@ def particle_exchange(geom, P, vol, conc, dt, xpar, pl=None, params=None, use_re
     if rc != BMXG_OK:
         raise RuntimeError(f"particle exchange failed: {rc}")
     return c.reshape(3, P.n)
+
+
+def split_cells(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, use_ref=False,
+                split_prob=0.1, split_len=0.0030):
+    """YEAST division on AoS records (numpy, abi.aos_dtype(34, 35), room for the
+    daughters), in place.  use_ref runs the reference's own split loop bodies
+    (draws only; split_prob / split_len feed its FUNGI branches).  Returns
+    (rc, number of divisions)."""
+    out = C.c_int64(0)
+    ptr = records.ctypes.data_as(C.c_void_p)
+    if draws is not None:
+        draws = np.ascontiguousarray(draws, dtype=np.float64)
+    dptr = None if draws is None else draws.ctypes.data_as(C.c_void_p)
+    nd = 0 if draws is None else draws.size
+    if use_ref:
+        used = C.c_int64(0)
+        rc = _quiet(lambda: reflib().ref_split_cells_aos(ptr, int(n), len(records), C.byref(sp), split_prob,
+                                                         split_len, dptr, nd, int(next_id), int(my_proc),
+                                                         C.byref(out), C.byref(used)))
+    else:
+        rc = lib().orc_split_cells_aos(C.byref(sp), ptr, int(n), len(records), 34, 35, dptr, nd,
+                                       int(seed) & (2**64 - 1), int(next_id), int(my_proc), C.byref(out))
+    return rc, out.value
+
+
+def split_uniform(seed, ident, cpu, j):
+    """Draw j of the seeded counter generator for the cell (ident, cpu)."""
+    return lib().orc_split_uniform(int(seed) & (2**64 - 1), int(ident), int(cpu), int(j))
+

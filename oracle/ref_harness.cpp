@@ -79,6 +79,23 @@ struct NbrIter {
     }
     int index() const { return idx[t]; }
 };
+// amrex::Particle<MAX_CHEM_REAL_VAR, MAX_CHEM_INT_VAR> of AMReX 22.x as the
+// split loop uses it, byte for byte: pos, rdata, id, cpu, idata (448 bytes).
+struct SplitParticle {
+    double m_pos[3];
+    double m_rdata[MAX_CHEM_REAL_VAR];
+    int m_id, m_cpu;
+    int m_idata[MAX_CHEM_INT_VAR];
+    double &pos(int d) { return m_pos[d]; }
+    double &rdata(int k) { return m_rdata[k]; }
+    int &idata(int k) { return m_idata[k]; }
+    int &id() { return m_id; }
+    int &cpu() { return m_cpu; }
+};
+struct BMXParticleContainer {
+    using ParticleType = SplitParticle;
+};
+
 struct NbrRange {
     NbrIter b, e;
     NbrIter begin() const { return b; }
@@ -349,6 +366,47 @@ void ref_surface_force(const bmxg_params *prm, const bmxg_particles *p, int64_t 
     std::vector<Real> fpar = force_params(prm);
     Real pos[3] = {p->x[i], p->y[i], p->z[i]};
     evaluateSurfaceForce(pos, &parts[i].rdata(0), &parts[i].idata(0), vel, rot, fpar.data());
+}
+
+// split_particles (src/des/bmx_split_particles.cpp:16-166) on one tile of
+// BMX's own particle structs: the flag loop body (:47-54, checkSplit) and the
+// fill loop body (:90-159, setNewCell / setNewSegment / setNewSegments) run as
+// the serial CPU build runs them, over an engine that hands out draws[] in call
+// order; the scan and the daughters' slots n + offset[i] as at :57-75.
+// Daughters past cap return BMXG_ERR_CAPACITY before any write.
+int ref_split_cells_aos(void *particles, int64_t n, int64_t cap, const bmxg_split_params *sp,
+                        double split_prob, double split_len, const double *draws, int64_t ndraws,
+                        int64_t next_id, int32_t my_proc, int64_t *num_split, int64_t *draws_used)
+{
+    if (!particles || !sp || !num_split || n < 0 || cap < n) return BMXG_ERR_ARG;
+    using ParticleType = SplitParticle;
+    static_assert(sizeof(SplitParticle) == 448, "AMReX 22.x particle layout");
+    ParticleType *pstruct = static_cast<ParticleType *>(particles);
+    const int np = (int)n;
+    const Real l_max_vol = sp->max_vol, l_max_len = sp->max_len, l_max_rad = sp->max_rad;
+    const Real l_brnch_prob = sp->brnch_prob, l_split_prob = split_prob, l_overlap = sp->overlap;
+    const int l_num_reals = sp->num_reals, l_num_ints = sp->num_ints;
+    long drawn = 0;
+    amrex::RandomEngine engine;
+    engine.u = draws;
+    engine.n = (long)ndraws;
+    engine.k = &drawn;
+    std::vector<unsigned int> do_split((size_t)np + 1, 0u);
+    unsigned int *do_split_p = do_split.data();
+    for (int i = 0; i < np; ++i) {
+#include "split_flag_body.inc"
+    }
+    std::vector<unsigned int> offsets((size_t)np + 1, 0u);
+    for (int i = 0; i < np; ++i) offsets[(size_t)i + 1] = offsets[(size_t)i] + do_split[(size_t)i];
+    *num_split = offsets[(size_t)np];
+    if (n + *num_split > cap) return BMXG_ERR_CAPACITY;
+    const long long next_pid = next_id;
+    const unsigned int *poffsets = offsets.data();
+    for (int pid = 0; pid < np; ++pid) {
+#include "split_fill_body.inc"
+    }
+    if (draws_used) *draws_used = drawn;
+    return BMXG_OK;
 }
 
 } // extern "C"

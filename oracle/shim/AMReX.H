@@ -17,10 +17,19 @@
 namespace amrex {
 using Real = double;
 template <class T> using Vector = std::vector<T>;
-// bmx_chem_K.H's segment-splitting and fusion kernels take a random engine;
-// the exchange kernels the oracle uses do not call it
-struct RandomEngine {};
-inline Real Random(RandomEngine const &) { return 0.5; }
+// bmx_chem_K.H's splitting and fusion kernels take a random engine; the
+// harness hands them a fixed sequence of draws (u[0], u[1], ... in call
+// order), and 0.5 once the sequence is used up or absent
+struct RandomEngine {
+    const double *u = nullptr;
+    long n = 0;
+    long *k = nullptr;
+};
+inline Real Random(RandomEngine const &e)
+{
+    if (!e.u || !e.k || *e.k >= e.n) return 0.5;
+    return e.u[(*e.k)++];
+}
 inline void Abort(const char *msg) { std::fprintf(stderr, "%s\n", msg); std::abort(); }
 }
 #endif

@@ -79,3 +79,58 @@ def within(a, b, rel, floor):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.abs(a - b).max()) <= rel * float(np.abs(b).max()) + floor
+
+
+# YEAST division inputs -------------------------------------------------------
+
+SPLIT_MAX_VOL = 5.0e-10  # SPECIES::max_vol of the size the yeast decks use (m^3)
+
+
+def split_params(**kw):
+    """bmxg_split_params of BMX's defaults: overlap 0.2, 3 species (9 reals
+    past first_data), no extra ints; FUNGI limits of bmx_chem_species_parms.cpp."""
+    from boltzmannmfx_gb300.abi import SplitParams
+    sp = SplitParams(max_vol=SPLIT_MAX_VOL, overlap=0.2, max_len=0.0035, max_rad=0.00025,
+                     brnch_prob=0.0, num_reals=9, num_ints=0)
+    for k, v in kw.items():
+        setattr(sp, k, v)
+    return sp
+
+
+def split_records(n, cap, seed, frac_divide=0.3, frac_fungi=0.2):
+    """Seeded AoS records (abi.aos_dtype(34, 35)): YEAST cells with volumes
+    around max_vol (about frac_divide of them above it), radius, area from the
+    volume, every other real and int filled with seeded values so that the
+    copy is checked whole, FUNGI interior segments mixed in (they never
+    divide), and the daughter slots [n, cap) filled with a sentinel pattern."""
+    from boltzmannmfx_gb300.abi import FUNGI, INT_IDX as I, REAL_IDX as R, YEAST, aos_dtype
+    rng = np.random.default_rng(seed)
+    a = np.zeros(cap, aos_dtype())
+    a["pos"][:n] = rng.uniform(-1.0e-3, 1.0e-3, (n, 3))
+    a["rdata"][:n] = rng.normal(0.0, 1.0, (n, 34))
+    a["idata"][:n] = rng.integers(-1000, 1000, (n, 35))
+    vol = SPLIT_MAX_VOL * np.where(rng.random(n) < frac_divide, rng.uniform(1.0001, 1.9, n),
+                                   rng.uniform(0.4, 1.0, n))
+    r = (3.0 * vol / (4.0 * np.pi)) ** (1.0 / 3.0)
+    a["rdata"][:n, R["vol"]] = vol
+    a["rdata"][:n, R["radius"]] = r
+    a["rdata"][:n, R["area"]] = 4.0 * np.pi * r * r
+    a["rdata"][:n, R["dvdt"]] = rng.uniform(0.0, 1.0e-12, n)
+    fungi = rng.random(n) < frac_fungi
+    a["idata"][:n, I["cell_type"]] = np.where(fungi, FUNGI, YEAST)
+    a["idata"][:n, I["position"]] = np.where(fungi, 3, rng.integers(0, 4, n))
+    a["id"][:n] = np.arange(1, n + 1)
+    a["cpu"][:n] = rng.integers(0, 4, n)
+    a["idata"][:n, I["id"]] = a["id"][:n]
+    a["idata"][:n, I["cpu"]] = a["cpu"][:n]
+    a["pos"][n:] = -3.0
+    a["rdata"][n:] = -7.0
+    a["id"][n:] = -5
+    a["cpu"][n:] = -6
+    a["idata"][n:] = -9
+    return a
+
+
+def split_expected_count(a, n, max_vol=SPLIT_MAX_VOL):
+    from boltzmannmfx_gb300.abi import INT_IDX as I, REAL_IDX as R, YEAST
+    return int(np.count_nonzero((a["idata"][:n, I["cell_type"]] == YEAST) & (a["rdata"][:n, R["vol"]] > max_vol)))

@@ -26,6 +26,9 @@ Cases:
   exchange       ParticleExchange (bmx_pc_xchng.cpp:122-151 + bmx_chem_K.H) on the
                  network below with seeded concentrations, a gentle and a
                  clamping mass-transfer rate
+  split_cells    split_particles (bmx_split_particles.cpp:47-54, :90-159 +
+                 checkSplit / setNewCell) on 96 AoS records, YEAST cells around
+                 max_vol with FUNGI interior segments mixed in, seeded draws
   fungi_network  the 410-segment hyphal network of the reference's checkpoint
                  exec/fungi/chk357900 (level 2, read with bmxg_read_checkpoint),
                  deck exec/fungi/input_fungi, 5 steps at the stable rod step
@@ -310,10 +313,25 @@ def exchange():
     print("exchange:", P.n)
 
 
+def split_cells():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from common import split_expected_count, split_params, split_records
+    n, cap = 96, 160
+    a = split_records(n, cap, 41)
+    k = split_expected_count(a, n)
+    draws = np.random.default_rng(43).random(2 * k)
+    out = a.copy()
+    rc, ns = O.split_cells(out, n, split_params(), draws=draws, use_ref=True)
+    assert rc == 0 and ns == k
+    np.savez_compressed(os.path.join(OUT, "split_cells.npz"), in_rec=a, out_rec=out, draws=draws,
+                        n=np.array(n), num_split=np.array(ns))
+    print("split_cells:", n, ns)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.have_ref():
         sys.exit("reference harness not built (reference tree missing?)")
     for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance,
-              init_bonds, fungi_network, exchange):
+              init_bonds, fungi_network, exchange, split_cells):
         f()
