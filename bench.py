@@ -4,7 +4,7 @@ with the plain FP64 form on the same workload beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload colonies|sphere_fp32|sphere_plain|rod_trees]
-                  [--precision fp32f|fp64]
+                  [--precision fp32f|fp64] [--only-split]
 
 `value`  device-resident throughput: K steps replayed from the captured step
          graph, timed with CUDA events on the context's stream (inputs are
@@ -51,6 +51,8 @@ def parse():
                     choices=["colonies", "sphere_fp32", "sphere_plain", "rod_trees"])
     ap.add_argument("--precision", default=None, choices=[None, "fp32f", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--only-split", action="store_true",
+                    help="print only the YEAST-division measurement (2 731 333 records, 5 %% dividing)")
     return ap.parse_args()
 
 
@@ -506,7 +508,11 @@ def run_ours(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.only_split:
+        from boltzmannmfx_gb300 import build, configs
+        build.build()
+        print(json.dumps(split_cost(2731333, configs.SEED + 2)), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

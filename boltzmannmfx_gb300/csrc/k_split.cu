@@ -65,8 +65,10 @@ __device__ __forceinline__ int split_kind(const SplitArgs &a, long long i)
     unsigned char *rec = a.par + i * a.stride;
     const int *q = rec_i(a, rec);
     const double *r = rec_r(a, rec);
+    // both words in flight together: they sit in different sectors of the record
     const int ct = q[I_cell_type];
-    if (ct == BMXG_YEAST) return r[R_vol] > a.max_vol ? 1 : 0;
+    const double vol = r[R_vol];
+    if (ct == BMXG_YEAST) return vol > a.max_vol ? 1 : 0;
     if (ct == BMXG_FUNGI) {
         const int pos = q[I_position];
         if (pos == BMXG_SITE_TIP)
@@ -167,9 +169,12 @@ __device__ void divide(const SplitArgs &a, long long i, long long k)
     double theta = 2.0 * u1 - 1.0;
     theta = acos(theta);
     const double phi = 2.0 * M_PI * u2;
-    const double nx = sin(theta) * cos(phi);
-    const double ny = sin(theta) * sin(phi);
-    const double nz = cos(theta);
+    double st, ct, sp, cp;
+    sincos(theta, &st, &ct);
+    sincos(phi, &sp, &cp);
+    const double nx = st * cp;
+    const double ny = st * sp;
+    const double nz = ct;
     const double scale = 1.0 - a.overlap;
     dp[0] = x + scale * 0.5 * nx * radius;
     dp[1] = y + scale * 0.5 * ny * radius;
@@ -223,27 +228,54 @@ __global__ void __launch_bounds__(kBlock) k_split_index(SplitArgs a, int *list)
 // sin / cos / pow of a division run with full warps (a few percent of the
 // cells divide in a step; one thread per cell would leave most lanes idle).
 // First the warp copies the copied block (copyChildParameters) of its 32
-// mothers into their daughters one record at a time, lane by lane along the
-// record, so the 448-byte records move in coalesced rows.
-__global__ void __launch_bounds__(kBlock) k_split_divide(SplitArgs a, const int *list, long long total)
+// mothers into their daughters: the (record, word) pairs are spread over the
+// lanes, kCopyUnroll loads in flight per lane before their stores, so the copy
+// costs a few memory round trips rather than one per record.  Small blocks
+// (kDivBlock): a step divides a few thousand cells, which must still cover
+// every SM.
+constexpr int kDivBlock = 64;
+constexpr int kCopyUnroll = 8;
+
+template <typename T>
+__device__ __forceinline__ void copy_block(const SplitArgs &a, const int *mothers, long long k0, int nk, int lane,
+                                           int nwords, int off)
 {
-    const long long k0 = (long long)blockIdx.x * kBlock + (threadIdx.x & ~31);
+    const int total = nk * nwords;
+    for (int t0 = lane; t0 < total; t0 += 32 * kCopyUnroll) {
+        T v[kCopyUnroll];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u) {
+            const int t = t0 + 32 * u;
+            if (t < total) {
+                const int j = t / nwords, w = t - j * nwords;
+                v[u] = ((const T *)(a.par + (long long)mothers[j] * a.stride + off))[w];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u) {
+            const int t = t0 + 32 * u;
+            if (t < total) {
+                const int j = t / nwords, w = t - j * nwords;
+                ((T *)(a.kid + (k0 + j) * a.stride + off))[w] = v[u];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kDivBlock) k_split_divide(SplitArgs a, const int *list, long long total)
+{
+    __shared__ int mothers[kDivBlock];
+    const long long k0 = (long long)blockIdx.x * kDivBlock + (threadIdx.x & ~31);
     if (k0 >= total) return;
     const int lane = threadIdx.x & 31;
     const long long k = k0 + lane;
     const int mine = k < total ? list[k] : 0;
+    int *wm = mothers + (threadIdx.x & ~31);
+    wm[lane] = mine;
+    __syncwarp();
     const int nk = total - k0 < 32 ? (int)(total - k0) : 32;
-    for (int j = 0; j < nk; ++j) {
-        const int i = __shfl_sync(0xffffffffu, mine, j);
-        unsigned char *mrec = a.par + (long long)i * a.stride;
-        unsigned char *drec = a.kid + (k0 + j) * a.stride;
-        const double *mr = rec_r(a, mrec);
-        double *dr = rec_r(a, drec);
-        const int *mi = rec_i(a, mrec);
-        int *di = rec_i(a, drec);
-        for (int w = lane; w < a.nreals; w += 32) dr[w] = mr[w];
-        for (int w = lane; w < a.nints; w += 32) di[w] = mi[w];
-    }
+    copy_block<double>(a, wm, k0, nk, lane, a.nreals, a.rdata);
+    copy_block<int>(a, wm, k0, nk, lane, a.nints, a.idata);
     __syncwarp();
     if (k < total) divide(a, mine, k);
 }
@@ -393,7 +425,7 @@ extern "C" int bmxg_split_cells_aos(const bmxg_split_params *sp, void *particles
         }
     }
     k_split_index<<<(unsigned)nb, kBlock, 0, st>>>(a, list);
-    k_split_divide<<<(unsigned)((total + kBlock - 1) / kBlock), kBlock, 0, st>>>(a, list, total);
+    k_split_divide<<<(unsigned)((total + kDivBlock - 1) / kDivBlock), kDivBlock, 0, st>>>(a, list, total);
     SPLIT_CK(cudaGetLastError());
     if (where == BMXG_HOST) {
         SPLIT_CK(cudaMemcpyAsync(particles, a.par, rec_bytes, cudaMemcpyDeviceToHost, st));
