@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--precision", default=None, choices=[None, "fp32f", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only-split", action="store_true",
-                    help="print only the YEAST-division measurement (2 731 333 records, 5 %% dividing)")
+                    help="print only the cell-division measurements (2 731 333 records, YEAST and FUNGI)")
     return ap.parse_args()
 
 
@@ -189,30 +189,52 @@ def adjoint_cost(Context, configs, BMXG_FP64, nsteps=200, ckpt=20):
             "adjoint_over_forward": b_ms / f_ms, "adjoint_over_plain_fp64": b_ms / p_ms}
 
 
-def split_cost(n, seed, reps=10, frac=0.05):
-    """YEAST division (bmxg_split_cells_aos) on n device-resident AoS records
-    (BMX's 448-byte particles, about frac of them above max_vol, seeded draws):
-    device time per call with CUDA events around it on torch's stream (each
-    call on a fresh copy of the records; the call includes its host read of the
-    division count), the host-buffer call's wall time, and the oracle on the
-    same records on one host core.  Algorithmic bytes per call: 12 B per record
-    per flag pass (cell_type 4 + vol 8, two passes) + 968 B per division (the
-    mother read 444, her changed fields written 80, the daughter written 444)."""
+def split_cost(n, seed, reps=10, frac=0.05, fungi=False):
+    """Cell division (bmxg_split_cells_aos) on n device-resident AoS records
+    (BMX's 448-byte particles, seeded draws): YEAST cells with about frac of
+    them above max_vol, or (fungi) hyphal segments in every state checkSplit
+    looks at, about frac of them dividing.  Device time per call with CUDA
+    events around it on torch's stream (each call on a fresh copy of the
+    records; the call includes its host reads of the totals), the host-buffer
+    call's wall time, and the oracle on the same records on one host core.
+    Algorithmic bytes per call: 12 B per record for the decision (cell_type 4
+    + vol 8; FUNGI segments also position, n_bnds, radius, c_length) + 1 B per
+    record of decisions written and read back + 968 B per new particle (the
+    mother read 444, her changed fields written 80, the daughter written
+    444)."""
     import torch
     from boltzmannmfx_gb300 import runtime
-    from boltzmannmfx_gb300.abi import BMXG_DEVICE, INT_IDX, REAL_IDX, SplitParams, aos_dtype
+    from boltzmannmfx_gb300.abi import BMXG_DEVICE, FUNGI, INT_IDX, REAL_IDX, SplitParams, aos_dtype
     from oracle import oracle as O
-    sp = SplitParams(max_vol=5.0e-10, overlap=0.2, max_len=0.0035, max_rad=0.00025, brnch_prob=0.0,
-                     num_reals=9, num_ints=0)
+    sp = SplitParams(max_vol=5.0e-10, overlap=0.2, max_len=0.0035, max_rad=0.00025,
+                     brnch_prob=0.05 if fungi else 0.0, split_prob=0.1, split_len=0.0030, num_reals=9,
+                     num_ints=0)
     rng = np.random.default_rng(seed)
-    cap = n + n // 8
+    cap = n + n // 4
     a = np.zeros(cap, aos_dtype())
     a["pos"][:n] = rng.uniform(-1.0e-3, 1.0e-3, (n, 3))
-    vol = 5.0e-10 * np.where(rng.random(n) < frac, rng.uniform(1.0001, 1.9, n), rng.uniform(0.4, 1.0, n))
-    r = (3.0 * vol / (4.0 * np.pi)) ** (1.0 / 3.0)
-    a["rdata"][:n, REAL_IDX["vol"]] = vol
-    a["rdata"][:n, REAL_IDX["radius"]] = r
-    a["rdata"][:n, REAL_IDX["area"]] = 4.0 * np.pi * r * r
+    if fungi:
+        # tips (a third at the length and radius limits), segments behind a
+        # tip, interior segments; frac sets the share of tips at the limits
+        pos = rng.integers(0, 4, n)
+        at = rng.random(n) < 3.0 * frac
+        L = np.where(at, 0.0036, 0.0030)
+        rad = np.where(at, 0.00026, 0.00020)
+        a["idata"][:n, INT_IDX["cell_type"]] = FUNGI
+        a["idata"][:n, INT_IDX["position"]] = pos
+        a["idata"][:n, INT_IDX["n_bnds"]] = np.where(pos == 3, 2, 1)
+        a["idata"][:n, 15] = rng.integers(1, 3, n)
+        a["rdata"][:n, REAL_IDX["c_length"]] = L
+        a["rdata"][:n, REAL_IDX["radius"]] = rad
+        a["rdata"][:n, REAL_IDX["theta"]] = rng.uniform(0.3, np.pi - 0.3, n)
+        a["rdata"][:n, REAL_IDX["phi"]] = rng.uniform(0.0, 2.0 * np.pi, n)
+        a["rdata"][:n, REAL_IDX["vol"]] = np.pi * rad * rad * L
+    else:
+        vol = 5.0e-10 * np.where(rng.random(n) < frac, rng.uniform(1.0001, 1.9, n), rng.uniform(0.4, 1.0, n))
+        r = (3.0 * vol / (4.0 * np.pi)) ** (1.0 / 3.0)
+        a["rdata"][:n, REAL_IDX["vol"]] = vol
+        a["rdata"][:n, REAL_IDX["radius"]] = r
+        a["rdata"][:n, REAL_IDX["area"]] = 4.0 * np.pi * r * r
     a["id"][:n] = np.arange(1, n + 1)
     a["idata"][:n, INT_IDX["id"]] = a["id"][:n]
     pristine = torch.from_numpy(a.view(np.uint8)).cuda()
@@ -242,15 +264,16 @@ def split_cost(n, seed, reps=10, frac=0.05):
     t0 = time.perf_counter()
     rc, kc = O.split_cells(h, n, sp, seed=0, next_id=n + 1)
     cpu_s = time.perf_counter() - t0
-    alg = 24 * n + 968 * k
+    alg = 14 * n + 968 * k
     peak, _ = measured_peak()
-    return {"call": "bmxg_split_cells_aos (device records)", "records": n, "divisions": k,
+    return {"call": "bmxg_split_cells_aos (device records)", "records": n,
+            "kind": "FUNGI segments" if fungi else "YEAST cells", "new_particles": k,
             "ms_per_call": ms, "records_per_s": n / (ms * 1e-3),
             "alg_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
             "frac_of_measured_hbm": (alg / (ms * 1e-3) / 1e9) / peak if peak else None,
             "host_records_ms": 1e3 * float(np.median(host_s)),
             "cpu_baseline": {"kind": "port", "cores": 1, "ms_per_call": 1e3 * cpu_s,
-                             "records_per_s": n / cpu_s, "rc": rc, "divisions": kc}}
+                             "records_per_s": n / cpu_s, "rc": rc, "new_particles": kc}}
 
 
 def cpu_baseline(w, budget_s=12.0):
@@ -468,7 +491,7 @@ def run_ours(args):
     split = None
     if rank == 0 and w.name.startswith("colonies"):
         adj = adjoint_cost(Context, configs, BMXG_FP64)
-        split = split_cost(N, configs.SEED + 2)
+        split = [split_cost(N, configs.SEED + 2), split_cost(N, configs.SEED + 3, fungi=True)]
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -512,6 +535,7 @@ def main():
         from boltzmannmfx_gb300 import build, configs
         build.build()
         print(json.dumps(split_cost(2731333, configs.SEED + 2)), flush=True)
+        print(json.dumps(split_cost(2731333, configs.SEED + 3, fungi=True)), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -81,10 +81,10 @@ class Stats(C.Structure):
 
 
 class SplitParams(C.Structure):
-    """bmxg_split_params: parameters of the YEAST division step."""
+    """bmxg_split_params: parameters of the division step."""
     _fields_ = [("max_vol", C.c_double), ("overlap", C.c_double), ("max_len", C.c_double),
-                ("max_rad", C.c_double), ("brnch_prob", C.c_double),
-                ("num_reals", C.c_int32), ("num_ints", C.c_int32)]
+                ("max_rad", C.c_double), ("brnch_prob", C.c_double), ("split_prob", C.c_double),
+                ("split_len", C.c_double), ("num_reals", C.c_int32), ("num_ints", C.c_int32)]
 
 
 # positions in amrex::Particle's rdata / idata (realIdx, intIdx of

@@ -317,54 +317,56 @@ int  bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overfl
 int  bmxg_particle_exchange(bmxg_ctx *ctx, const double *vol, double *conc, double dt,
                             const double xpar[3], int32_t where);
 
-/* ---- YEAST cell division ------------------------------------------------- */
+/* ---- cell division ------------------------------------------------------- */
 
 /* Parameters of the division step (SPECIES::max_vol, max_seg_length,
- * max_seg_radius, branching_probability of src/mods/bmx_chem_species_parms.cpp:
- * 55-70; BMXChemistry::p_overlap, p_num_reals, p_num_ints of
- * src/chemistry/bmx_chem.cpp:29-53,110). */
+ * max_seg_radius, branching_probability, split_probability, seg_split_length
+ * of src/mods/bmx_chem_species_parms.cpp:55-70; BMXChemistry::p_overlap,
+ * p_num_reals, p_num_ints of src/chemistry/bmx_chem.cpp:29-53,110). */
 typedef struct bmxg_split_params {
     double  max_vol;     /* a YEAST cell with vol > max_vol divides                       */
     double  overlap;     /* p_overlap (0.2): mother and daughter overlap by this fraction */
-    double  max_len;     /* FUNGI: tip length at which the reference splits a tip          */
-    double  max_rad;     /* FUNGI: tip radius at which the reference splits a tip          */
-    double  brnch_prob;  /* FUNGI: per-step side-branch probability                       */
+    double  max_len;     /* a FUNGI tip at least this long ...                            */
+    double  max_rad;     /* ... and at least this wide splits                             */
+    double  brnch_prob;  /* a segment behind a tip branches with this probability         */
+    double  split_prob;  /* a splitting tip with bonds splits in two with 1 - this        */
+    double  split_len;   /* length a splitting tip keeps                                  */
     int32_t num_reals;   /* p_num_reals (3 x species): reals copied past first_data        */
     int32_t num_ints;    /* p_num_ints (0): ints copied past first_data                    */
 } bmxg_split_params;
 
-/* The YEAST part of BMXParticleContainer::split_particles
- * (src/des/bmx_split_particles.cpp:16-166, with checkSplit, copyChildParameters
- * and setNewCell of src/chemistry/bmx_chem_K.H:23-69,357-440) on particles in
- * the reference's own layout (the AoS records of bmxg_evolve_particles_aos,
- * nreal >= 34, nint >= 35).  Every YEAST cell with vol > max_vol divides: a
- * daughter is appended at particles[n + k], k = the number of dividing cells
- * before it in array order (the reference's exclusive scan), with id
- * next_id + k and cpu my_proc; mother and daughter move apart by
- * (1 - overlap) r along a random direction and each gets half the volume,
- * the radius, area and dadt of that volume, and half of the species
- * increments (first_data + 6..8).  The direction of division k comes from
- * draws[2k] (cos theta = 2 u - 1) and draws[2k + 1] (phi = 2 pi u), values
- * in [0, 1) that the caller draws, e.g. with amrex::Random, in that order; with
- * draws == NULL they come from a SplitMix64 counter generator keyed by seed
- * and the mother's id and cpu, the same on every device and host.  Fields the
- * reference leaves unset in a daughter (reals and ints past the copied
- * block) are not written.
- * FUNGI segments are never divided here: when one meets the reference's
- * tip-split (TIP, radius >= max_rad, c_length >= max_len) or side-branch
- * (SECOND_1 / SECOND_2 with brnch_prob > 0) condition the call returns
- * BMXG_ERR_UNSUPPORTED and writes nothing.
- * *num_split receives the number of divisions.  When n + *num_split > cap,
- * or draws holds fewer than 2 * *num_split values (ndraws), the call returns
+/* BMXParticleContainer::split_particles (src/des/bmx_split_particles.cpp:16-166,
+ * with checkSplit, copyChildParameters, setNewCell, setNewSegment and
+ * setNewSegments of src/chemistry/bmx_chem_K.H:23-69,357-1011,2129-2494) on
+ * particles in the reference's own layout (the AoS records of
+ * bmxg_evolve_particles_aos, nreal >= 34, nint >= 35):
+ *  - a YEAST cell with vol > max_vol divides in two along a random direction;
+ *  - a FUNGI tip with radius >= max_rad and c_length >= max_len either grows a
+ *    new tip (or halves, when it has no bonds) or, with probability
+ *    1 - split_prob, splits into two tips;
+ *  - a FUNGI segment right behind a tip grows a side branch with probability
+ *    brnch_prob.
+ * New particles are appended at particles[n + k], k counting the new particles
+ * before them in array order (the reference's exclusive scan; a two-way split
+ * appends two), with id next_id + k and cpu my_proc.
+ * Random draws: `draws` (ndraws values in [0, 1)) is the sequence a serial run
+ * of the reference takes from amrex::Random, in its order: one per FUNGI tip
+ * at the radius limit and per segment behind a tip (checkSplit, array order),
+ * then per division in array order 2 (YEAST cell), 2 (new tip), 3 (side
+ * branch), 4 (two-way split) or 0 (isolated segment).  With draws == NULL a
+ * SplitMix64 counter generator keyed by seed and the cell's id and cpu
+ * supplies them, the same on every device and host.  Fields the reference
+ * leaves unset in a new particle are not written.
+ * *num_split receives the number of new particles.  When n + *num_split > cap,
+ * or draws holds fewer values than the call takes, the call returns
  * BMXG_ERR_CAPACITY or BMXG_ERR_ARG and writes nothing else.  where:
  * BMXG_HOST (particles and draws in host memory) or BMXG_DEVICE (device
  * memory).  Runs on `stream` (NULL = legacy default stream) and returns after
- * it completes; the host reads the division count in between, as the
- * reference does (bmx_split_particles.cpp:58-66).  Each device keeps a
- * scratch of about 4.2 bytes per particle of the largest call so far (and
- * 8 bytes of pinned host memory) until the process exits; calls on one
- * device run one at a time.  Host-memory calls also stage the records on the
- * device for the length of the call. */
+ * it completes; the host reads the totals in between, as the reference does
+ * (bmx_split_particles.cpp:58-66).  Each device keeps a scratch of about 17
+ * bytes per particle of the largest call so far (and 32 bytes of pinned host
+ * memory) until the process exits; calls on one device run one at a time.
+ * Host-memory calls also stage the records on the device for the call. */
 int  bmxg_split_cells_aos(const bmxg_split_params *sp, void *particles, int64_t n, int64_t cap,
                           int32_t nreal, int32_t nint, const double *draws, int64_t ndraws,
                           uint64_t seed, int64_t next_id, int32_t my_proc, int32_t where,

@@ -977,13 +977,17 @@ int orc_particle_exchange(const bmxg_geometry *geom, const bmxg_particles *p, co
 }
 
 /* ------------------------------------------------------------------------ */
-/* YEAST division (split_particles)                                          */
+/* cell division (split_particles)                                           */
 /* ------------------------------------------------------------------------ */
 
 /* realIdx / intIdx positions the division touches (bmx_chem.H:38-118) */
-enum { SR_radius = 0, SR_c_length = 1, SR_area = 4, SR_vol = 5, SR_dadt = 21, SR_dvdt = 22,
-       SR_bond_scale = 24, SR_first = 25 };
-enum { SI_cell_type = 5, SI_position = 19, SI_fuse_tip = 25, SI_id = 33, SI_cpu = 34, SI_first = 35 };
+enum { SR_radius = 0, SR_c_length = 1, SR_theta = 2, SR_phi = 3, SR_area = 4, SR_vol = 5, SR_dadt = 21,
+       SR_dvdt = 22, SR_bond_scale = 24, SR_first = 25 };
+enum { SI_cell_type = 5, SI_n_bnds = 6, SI_seg1_id1 = 7, SI_seg2_id1 = 8, SI_seg3_id1 = 9, SI_seg4_id1 = 10,
+       SI_seg1_id2 = 11, SI_seg2_id2 = 12, SI_seg3_id2 = 13, SI_seg4_id2 = 14, SI_site1 = 15, SI_site2 = 16,
+       SI_site3 = 17, SI_site4 = 18, SI_position = 19, SI_fuse_flag = 20, SI_split_flag = 21,
+       SI_new_flag = 22, SI_fuse_id = 23, SI_fuse_cpu = 24, SI_fuse_tip = 25, SI_dltd_site1 = 26,
+       SI_fix_site = 32, SI_id = 33, SI_cpu = 34, SI_first = 35 };
 
 /* SplitMix64 (Steele, Lea and Flood, OOPSLA 2014) on the counter (cpu, id, j),
  * 53 bits to a double in [0, 1): the draws of the library's seeded mode. */
@@ -997,30 +1001,342 @@ double orc_split_uniform(uint64_t seed, int32_t id, int32_t cpu, int32_t j)
     return (double)(z >> 11) * 0x1.0p-53;
 }
 
-/* checkSplit (bmx_chem_K.H:23-69) without its draws: 1 = a YEAST cell with
- * vol > max_vol; 2 = a FUNGI tip long and wide enough to split, or a segment
- * behind a tip that may branch (outside the restated part); 0 = neither. */
-static int split_kind(const bmxg_split_params *sp, const double *r, const int *q)
+/* one record's views */
+typedef struct {
+    double *p, *r;
+    int *id, *q;
+} orec_t;
+
+/* the draws of one cell: the caller's sequence from *next, or the counter
+ * generator at (id, cpu, j0 + k) */
+typedef struct {
+    const double *seq;
+    int64_t *next;
+    uint64_t seed;
+    int id, cpu, j;
+} odraw_t;
+
+static double odraw(odraw_t *d)
 {
-    if (q[SI_cell_type] == BMXG_YEAST) return r[SR_vol] > sp->max_vol ? 1 : 0;
-    if (q[SI_cell_type] == BMXG_FUNGI) {
-        if (q[SI_position] == BMXG_SITE_TIP)
-            return (r[SR_radius] >= sp->max_rad && r[SR_c_length] >= sp->max_len) ? 2 : 0;
-        if (q[SI_position] == BMXG_SITE_SECOND_1 || q[SI_position] == BMXG_SITE_SECOND_2)
-            return sp->brnch_prob > 0.0 ? 2 : 0;
+    if (d->seq) return d->seq[(*d->next)++];
+    return orc_split_uniform(d->seed, d->id, d->cpu, d->j++);
+}
+
+/* checkSplit (bmx_chem_K.H:23-69): the draw it takes (FUNGI tip at the radius
+ * limit, segment behind a tip) and the new-particle count it returns */
+static int ocheck_draws(const bmxg_split_params *sp, const orec_t *m)
+{
+    if (m->q[SI_cell_type] != BMXG_FUNGI) return 0;
+    if (m->q[SI_position] == BMXG_SITE_TIP) return m->r[SR_radius] >= sp->max_rad;
+    return m->q[SI_position] == BMXG_SITE_SECOND_1 || m->q[SI_position] == BMXG_SITE_SECOND_2;
+}
+
+static int odecide(const bmxg_split_params *sp, const orec_t *m, double x)
+{
+    const int ct = m->q[SI_cell_type];
+    if (ct == BMXG_YEAST) return m->r[SR_vol] > sp->max_vol ? 1 : 0;
+    if (ct != BMXG_FUNGI) return 0;
+    if (m->q[SI_position] == BMXG_SITE_TIP) {
+        if (!(m->r[SR_radius] >= sp->max_rad) || !(m->r[SR_c_length] >= sp->max_len)) return 0;
+        return (x > sp->split_prob || m->q[SI_n_bnds] == 0) ? 1 : 2;
     }
+    if (m->q[SI_position] == BMXG_SITE_SECOND_1 || m->q[SI_position] == BMXG_SITE_SECOND_2)
+        return x < sp->brnch_prob ? 1 : 0;
     return 0;
 }
 
-/* Pass 1 counts the dividing cells (the scan's total, bmx_split_particles.cpp:
- * 44-66); pass 2 walks them in array order, daughter k at record n + k with id
- * next_id + k (:68-121): copyChildParameters (bmx_chem_K.H:357-370) copies
- * reals [0, first_data + num_reals) and ints [0, first_data + num_ints);
- * setNewCell (:383-440) moves mother and daughter apart by (1 - overlap) r / 2
- * each along n = (sin t cos p, sin t sin p, cos t), cos t = 2 u1 - 1,
- * p = 2 pi u2, halves the volume, sets radius, area and dadt from it, resets
- * the daughter's bond_scale and fuse_tip and halves both cells' species
- * increments first_data + 6..8. */
+/* setNewCell (bmx_chem_K.H:383-440): mother and daughter apart by
+ * (1 - overlap) r / 2 each along n = (sin t cos p, sin t sin p, cos t),
+ * cos t = 2 u1 - 1, p = 2 pi u2; half the volume each, radius, area and dadt
+ * of that volume, the daughter's bond_scale and fuse_tip reset, both cells'
+ * species increments first_data + 6..8 halved */
+static void odivide_cell(const bmxg_split_params *sp, orec_t *m, orec_t *d, odraw_t *u)
+{
+    const double x = m->p[0], y = m->p[1], z = m->p[2];
+    double radius = d->r[SR_radius];
+    const double theta = acos(2.0 * odraw(u) - 1.0);
+    const double phi = 2.0 * ORC_PI * odraw(u);
+    const double nx = sin(theta) * cos(phi), ny = sin(theta) * sin(phi), nz = cos(theta);
+    const double half = (1.0 - sp->overlap) * 0.5;
+    d->p[0] = x + half * nx * radius;
+    d->p[1] = y + half * ny * radius;
+    d->p[2] = z + half * nz * radius;
+    m->p[0] = x - half * nx * radius;
+    m->p[1] = y - half * ny * radius;
+    m->p[2] = z - half * nz * radius;
+    const double volume = m->r[SR_vol] / 2.0;
+    radius = pow(3.0 * volume / (4.0 * ORC_PI), 1.0 / 3.0);
+    const double area = 4.0 * ORC_PI * radius * radius;
+    const double dadt = 2.0 * m->r[SR_dvdt] / radius;
+    m->r[SR_vol] = d->r[SR_vol] = volume;
+    m->r[SR_area] = d->r[SR_area] = area;
+    m->r[SR_dadt] = d->r[SR_dadt] = dadt;
+    m->r[SR_radius] = d->r[SR_radius] = radius;
+    d->r[SR_bond_scale] = 1.0;
+    d->q[SI_fuse_tip] = 0;
+    for (int j = 6; j < 9; ++j) {
+        m->r[SR_first + j] = 0.5 * m->r[SR_first + j];
+        d->r[SR_first + j] = 0.5 * d->r[SR_first + j];
+    }
+}
+
+/* polar angles as the reference recovers a direction's: t = acos(z),
+ * p = acos(x / sin t), 2 pi - p for y < 0, p = 0 on the axis */
+static void oangles(double x, double y, double z, double *t, double *st, double *p)
+{
+    *t = acos(z);
+    *st = sin(*t);
+    *p = 0.0;
+    if (*st != 0.0) {
+        *p = acos(x / *st);
+        if (y < 0.0) *p = 2.0 * ORC_PI - *p;
+    }
+}
+
+/* a direction within 0.1 rad of the x axis (t = 0.1 u1, p = 2 pi u2) turned
+ * by the rotation that takes the x axis to (sin gt cos gp, sin gt sin gp,
+ * cos gt) */
+static void oaround(double gst, double gct, double gphi, odraw_t *u, double g[3])
+{
+    const double gcp = cos(gphi), gsp = sin(gphi);
+    const double R[3][3] = {{gcp * gst, -gsp, -gcp * gct}, {gsp * gst, gcp, -gsp * gct}, {gct, 0.0, gst}};
+    const double rt = 0.1 * odraw(u);
+    const double rp = 2.0 * ORC_PI * odraw(u);
+    const double v[3] = {cos(rt), sin(rt) * sin(rp), sin(rt) * cos(rp)};
+    for (int k = 0; k < 3; ++k) g[k] = R[k][0] * v[0] + R[k][1] * v[1] + R[k][2] * v[2];
+}
+
+static void otip_flags(int *q, int dltd, int newf)
+{
+    q[SI_position] = BMXG_SITE_TIP;
+    q[SI_fuse_flag] = 0;
+    q[SI_split_flag] = 0;
+    if (newf) q[SI_new_flag] = 0;
+    q[SI_fuse_id] = -1;
+    q[SI_fuse_cpu] = -1;
+    if (dltd)
+        for (int j = 0; j < 6; ++j) q[SI_dltd_site1 + j] = -1;
+}
+
+static void ocylinder(double *r)
+{
+    const double L = r[SR_c_length], a = r[SR_radius];
+    r[SR_vol] = ORC_PI * a * a * L;
+    r[SR_area] = 2.0 * ORC_PI * a * L + 2.0 * ORC_PI * a * a;
+}
+
+static void odir(const double *r, double n[3])
+{
+    n[0] = sin(r[SR_theta]) * cos(r[SR_phi]);
+    n[1] = sin(r[SR_theta]) * sin(r[SR_phi]);
+    n[2] = cos(r[SR_theta]);
+}
+
+/* setNewSegment (bmx_chem_K.H:457-1011).  The gradient is forced to zero
+ * (:468-473), so a tip grows along itself and a side branch leaves at +-45
+ * degrees (draw > 0.5: +) in the xy plane before the 0.1 rad scatter.
+ *  isolated (no bonds): two halves a quarter length either side, bonded;
+ *  tip: keeps split_len at its bonded end; the new tip of the remaining
+ *       length starts at the mother's new free end;
+ *  behind a tip: a 5e-4 branch at the end the tip hangs on; both radii shrink
+ *       to sqrt(V / (pi 2 L)) (the daughter still holds the mother's length,
+ *       :939).
+ * Bond tables, sites, positions and the flags of a new tip as the reference
+ * sets them; volume and area of both from length and radius. */
+static void odivide_segment(const bmxg_split_params *sp, orec_t *m, orec_t *d, odraw_t *u, int id, int cpu)
+{
+    const int nbnd = m->q[SI_n_bnds], position = m->q[SI_position];
+    double n[3];
+    odir(m->r, n);
+    const double c = m->r[SR_c_length];
+    double x[3] = {m->p[0], m->p[1], m->p[2]};
+    if (nbnd == 0) {
+        for (int k = 0; k < 3; ++k) {
+            m->p[k] = x[k] + 0.25 * c * n[k];
+            d->p[k] = x[k] - 0.25 * c * n[k];
+        }
+        m->r[SR_c_length] = d->r[SR_c_length] = 0.5 * c;
+        m->q[SI_n_bnds] = 1;
+        m->q[SI_seg1_id1] = id;
+        m->q[SI_seg1_id2] = cpu;
+        m->q[SI_site1] = 1;
+        otip_flags(m->q, 1, 1);
+        d->q[SI_n_bnds] = 1;
+        d->q[SI_seg1_id1] = m->q[SI_id];
+        d->q[SI_seg1_id2] = m->q[SI_cpu];
+        d->q[SI_site1] = 2;
+        otip_flags(d->q, 1, 1);
+        d->q[SI_fix_site] = 0;
+        for (int j = 6; j < 9; ++j) {
+            m->r[SR_first + j] = 0.5 * m->r[SR_first + j];
+            d->r[SR_first + j] = 0.5 * d->r[SR_first + j];
+        }
+    } else if (position == BMXG_SITE_TIP) {
+        const int bsite = m->q[SI_site1];
+        double gt, gst, gp, g[3], nt, nst, np;
+        oangles(n[0], n[1], n[2], &gt, &gst, &gp);
+        oaround(gst, n[2], gp, u, g);
+        const double sl = sp->split_len, rest = c - sl;
+        double e[3], f[3];
+        if (bsite == 1) {  /* keep the site-1 end, grow from the new site 2 */
+            for (int k = 0; k < 3; ++k) {
+                const double a = x[k] - 0.5 * c * n[k];
+                e[k] = a + sl * n[k];
+                m->p[k] = 0.5 * (a + e[k]);
+                f[k] = e[k] + g[k] * rest;
+            }
+            m->q[nbnd == 1 ? SI_site2 : SI_site3] = 2;
+            m->q[SI_position] = BMXG_SITE_SECOND_2;
+        } else {
+            for (int k = 0; k < 3; ++k) {
+                const double b = x[k] + 0.5 * c * n[k];
+                e[k] = b - sl * n[k];
+                m->p[k] = 0.5 * (e[k] + b);
+                f[k] = e[k] - g[k] * rest;
+            }
+            m->q[nbnd == 1 ? SI_site2 : SI_site3] = 1;
+            m->q[SI_position] = BMXG_SITE_SECOND_1;
+        }
+        m->r[SR_c_length] = sl;
+        for (int k = 0; k < 3; ++k) d->p[k] = 0.5 * (e[k] + f[k]);
+        d->r[SR_c_length] = rest;
+        oangles(g[0], g[1], g[2], &nt, &nst, &np);
+        d->r[SR_theta] = nt;
+        d->r[SR_phi] = np;
+        d->q[SI_site1] = bsite == 1 ? 1 : 2;
+        otip_flags(d->q, bsite == 1, 1);
+        d->q[SI_fix_site] = 0;
+        m->q[SI_n_bnds] = nbnd == 1 ? 2 : 3;
+        m->q[nbnd == 1 ? SI_seg2_id1 : SI_seg3_id1] = id;
+        m->q[nbnd == 1 ? SI_seg2_id2 : SI_seg3_id2] = cpu;
+        d->q[SI_n_bnds] = 1;
+        d->q[SI_seg1_id1] = m->q[SI_id];
+        d->q[SI_seg1_id2] = m->q[SI_cpu];
+        for (int j = 6; j < 9; ++j) d->r[SR_first + j] = 0.0;
+    } else if (position == BMXG_SITE_SECOND_1 || position == BMXG_SITE_SECOND_2) {
+        const double phi = m->r[SR_phi];
+        const double tphi = phi + (odraw(u) > 0.5 ? 0.25 * ORC_PI : -0.25 * ORC_PI);
+        double gt, gst, gp, g[3], nt, nst, np;
+        oangles(cos(tphi), sin(tphi), 0.0, &gt, &gst, &gp);
+        oaround(gst, 0.0, gp, u, g);
+        oangles(g[0], g[1], g[2], &nt, &nst, &np);
+        const double bl = 0.0005;
+        const int s1 = position == BMXG_SITE_SECOND_1;
+        if (nbnd == 2) m->q[SI_site3] = s1 ? 1 : 2;
+        else if (nbnd == 3) m->q[SI_site4] = s1 ? 1 : 2;
+        for (int k = 0; k < 3; ++k) {
+            const double end = s1 ? x[k] - 0.5 * c * n[k] : x[k] + 0.5 * c * n[k];
+            const double far = s1 ? end - g[k] * bl : end + g[k] * bl;
+            d->p[k] = 0.5 * (end + far);
+        }
+        d->q[SI_site1] = d->q[SI_site2] = s1 ? 2 : 1;
+        const double a0 = m->r[SR_radius];
+        const double v0 = c * a0 * a0 * ORC_PI;
+        d->r[SR_theta] = nt;
+        d->r[SR_phi] = np;
+        const double a1 = sqrt(v0 / (ORC_PI * (c + d->r[SR_c_length])));
+        m->r[SR_radius] = d->r[SR_radius] = a1;
+        d->r[SR_c_length] = bl;
+        m->q[SI_n_bnds] = nbnd == 2 ? 3 : 4;
+        m->q[nbnd == 2 ? SI_seg3_id1 : SI_seg4_id1] = id;
+        m->q[nbnd == 2 ? SI_seg3_id2 : SI_seg4_id2] = cpu;
+        d->q[SI_n_bnds] = 2;
+        d->q[SI_seg1_id1] = m->q[SI_id];
+        d->q[SI_seg1_id2] = m->q[SI_cpu];
+        d->q[SI_seg2_id1] = m->q[nbnd == 2 ? SI_seg2_id1 : SI_seg3_id1];
+        d->q[SI_seg2_id2] = m->q[nbnd == 2 ? SI_seg2_id2 : SI_seg3_id2];
+        otip_flags(d->q, 1, 1);
+        d->q[SI_fix_site] = 0;
+        m->q[SI_position] = BMXG_SITE_INTERIOR;
+        for (int j = 6; j < 9; ++j) d->r[SR_first + j] = 0.0;
+    }
+    d->q[SI_id] = id;
+    d->q[SI_cpu] = cpu;
+    ocylinder(m->r);
+    ocylinder(d->r);
+    d->r[SR_bond_scale] = 1.0;
+    d->q[SI_fuse_tip] = 0;
+}
+
+/* setNewSegments (bmx_chem_K.H:2129-2494): a tip keeps split_len at its bonded
+ * end; two tips of half the rest each leave its free end at phi +- 45 degrees
+ * in the xy plane (then the 0.1 rad scatter), bonded to the mother and to each
+ * other */
+static void odivide_tip_in_two(const bmxg_split_params *sp, orec_t *m, orec_t *d1, orec_t *d2, odraw_t *u,
+                               int id1, int cpu1, int id2, int cpu2)
+{
+    double n[3];
+    odir(m->r, n);
+    const double phi = m->r[SR_phi];
+    double gt, gst1, gp1, gst2, gp2, g1[3], g2[3], t1, st1, p1, t2, st2, p2;
+    oangles(cos(phi + 0.25 * ORC_PI), sin(phi + 0.25 * ORC_PI), 0.0, &gt, &gst1, &gp1);
+    oangles(cos(phi - 0.25 * ORC_PI), sin(phi - 0.25 * ORC_PI), 0.0, &gt, &gst2, &gp2);
+    oaround(gst1, 0.0, gp1, u, g1);
+    oaround(gst2, 0.0, gp2, u, g2);
+    oangles(g1[0], g1[1], g1[2], &t1, &st1, &p1);
+    oangles(g2[0], g2[1], g2[2], &t2, &st2, &p2);
+    const double c = m->r[SR_c_length];
+    const double half = 0.5 * (c - sp->split_len), keep = c - 2.0 * half;
+    const int s1 = m->q[SI_site1] == 1;
+    for (int k = 0; k < 3; ++k) {
+        const double x = m->p[k];
+        const double a = s1 ? x - 0.5 * c * n[k] : x + 0.5 * c * n[k];  /* the kept end */
+        const double b = s1 ? a + keep * n[k] : a - keep * n[k];        /* the new free end */
+        m->p[k] = 0.5 * (a + b);
+        d1->p[k] = 0.5 * (b + (s1 ? b + g1[k] * half : b - g1[k] * half));
+        d2->p[k] = 0.5 * (b + (s1 ? b + g2[k] * half : b - g2[k] * half));
+    }
+    const int site = s1 ? 1 : 2, msite = s1 ? 2 : 1;
+    int *q1 = d1->q, *q2 = d2->q;
+    q1[SI_site1] = q1[SI_site2] = site;
+    q1[SI_seg1_id1] = m->q[SI_id];
+    q1[SI_seg1_id2] = m->q[SI_cpu];
+    q1[SI_seg2_id1] = id2;
+    q1[SI_seg2_id2] = cpu2;
+    q1[SI_n_bnds] = 2;
+    q2[SI_site1] = q2[SI_site2] = site;
+    q2[SI_seg1_id1] = m->q[SI_id];
+    q2[SI_seg1_id2] = m->q[SI_cpu];
+    q2[SI_seg2_id1] = id1;
+    q2[SI_seg2_id2] = cpu1;
+    q2[SI_n_bnds] = 2;
+    const int one = m->q[SI_n_bnds] == 1;
+    m->q[one ? SI_site2 : SI_site3] = msite;
+    m->q[one ? SI_seg2_id1 : SI_seg3_id1] = id1;
+    m->q[one ? SI_seg2_id2 : SI_seg3_id2] = cpu1;
+    m->q[one ? SI_site3 : SI_site4] = msite;
+    m->q[one ? SI_seg3_id1 : SI_seg4_id1] = id2;
+    m->q[one ? SI_seg3_id2 : SI_seg4_id2] = cpu2;
+    m->q[SI_n_bnds] = one ? 3 : 4;
+    m->r[SR_c_length] = keep;
+    d1->r[SR_c_length] = d2->r[SR_c_length] = half;
+    d1->r[SR_theta] = t1;
+    d1->r[SR_phi] = p1;
+    d2->r[SR_theta] = t2;
+    d2->r[SR_phi] = p2;
+    otip_flags(q1, 1, 0);
+    q1[SI_fix_site] = 0;
+    otip_flags(q2, 1, 0);
+    q2[SI_fix_site] = 0;
+    m->q[SI_position] = BMXG_SITE_INTERIOR;
+    q1[SI_id] = id1;
+    q1[SI_cpu] = cpu1;
+    q2[SI_id] = id2;
+    q2[SI_cpu] = cpu2;
+    ocylinder(m->r);
+    ocylinder(d1->r);
+    d1->r[SR_bond_scale] = 1.0;
+    q1[SI_fuse_tip] = 0;
+    ocylinder(d2->r);
+    d2->r[SR_bond_scale] = 1.0;
+    q2[SI_fuse_tip] = 0;
+}
+
+/* split_particles (bmx_split_particles.cpp:16-166) run serially: checkSplit
+ * for every particle in array order (taking its draw there), the exclusive
+ * scan of the new-particle counts, and the fill loop in array order, new
+ * particle k at record n + k with id next_id + k, the divisions taking their
+ * draws in that order. */
 int orc_split_cells_aos(const bmxg_split_params *sp, void *particles, int64_t n, int64_t cap,
                         int32_t nreal, int32_t nint, const double *draws, int64_t ndraws,
                         uint64_t seed, int64_t next_id, int32_t my_proc, int64_t *num_split)
@@ -1038,61 +1354,60 @@ int orc_split_cells_aos(const bmxg_split_params *sp, void *particles, int64_t n,
     const size_t off_i = off_id + 2 * sizeof(int);
     const size_t stride = (off_i + (size_t)nint * sizeof(int) + 7) / 8 * 8;
     unsigned char *base = (unsigned char *)particles;
-#define REC(i) (base + (size_t)(i) * stride)
-    int64_t total = 0;
+#define OREC(i) ((orec_t){(double *)(base + (size_t)(i) * stride), (double *)(base + (size_t)(i) * stride + off_r), \
+                          (int *)(base + (size_t)(i) * stride + off_id), (int *)(base + (size_t)(i) * stride + off_i)})
+    signed char *nnew = (signed char *)malloc((size_t)n);
+    if (!nnew) return BMXG_ERR_OOM;
+    int64_t next = 0, total = 0, need = 0;
     for (int64_t i = 0; i < n; ++i) {
-        const int kind = split_kind(sp, (const double *)(REC(i) + off_r), (const int *)(REC(i) + off_i));
-        if (kind == 2) return BMXG_ERR_UNSUPPORTED;
-        total += kind;
+        const orec_t m = OREC(i);
+        double x = 0.0;
+        if (ocheck_draws(sp, &m)) {
+            if (draws && next >= ndraws) {
+                free(nnew);
+                return BMXG_ERR_ARG;
+            }
+            x = draws ? draws[next++] : orc_split_uniform(seed, m.id[0], m.id[1], 0);
+        }
+        nnew[i] = (signed char)odecide(sp, &m, x);
+        total += nnew[i];
+        if (nnew[i] == 2) need += 4;
+        else if (nnew[i] == 1)
+            need += m.q[SI_cell_type] == BMXG_YEAST ? 2
+                  : (m.q[SI_n_bnds] == 0 ? 0 : (m.q[SI_position] == BMXG_SITE_TIP ? 2 : 3));
     }
     *num_split = total;
-    if (total == 0) return BMXG_OK;
-    if (n + total > cap) return BMXG_ERR_CAPACITY;
-    if (draws && ndraws < 2 * total) return BMXG_ERR_ARG;
+    if (total == 0 || n + total > cap || (draws && ndraws < next + need)) {
+        free(nnew);
+        return total == 0 ? BMXG_OK : (n + total > cap ? BMXG_ERR_CAPACITY : BMXG_ERR_ARG);
+    }
     const int nreals = SR_first + sp->num_reals, nints = SI_first + sp->num_ints;
     int64_t k = 0;
     for (int64_t i = 0; i < n; ++i) {
-        unsigned char *m = REC(i), *d = REC(n + k);
-        double *mp = (double *)m, *dp = (double *)d;
-        double *mr = (double *)(m + off_r), *dr = (double *)(d + off_r);
-        int *mi = (int *)(m + off_i), *di = (int *)(d + off_i);
-        const int *mid = (const int *)(m + off_id);
-        int *did = (int *)(d + off_id);
-        if (split_kind(sp, mr, mi) != 1) continue;
-        for (int j = 0; j < nreals; ++j) dr[j] = mr[j];
-        for (int j = 0; j < nints; ++j) di[j] = mi[j];
-        const double u1 = draws ? draws[2 * k] : orc_split_uniform(seed, mid[0], mid[1], 0);
-        const double u2 = draws ? draws[2 * k + 1] : orc_split_uniform(seed, mid[0], mid[1], 1);
-        const double x = mp[0], y = mp[1], z = mp[2];
-        double radius = dr[SR_radius];
-        const double theta = acos(2.0 * u1 - 1.0);
-        const double phi = 2.0 * ORC_PI * u2;
-        const double nx = sin(theta) * cos(phi), ny = sin(theta) * sin(phi), nz = cos(theta);
-        const double half = (1.0 - sp->overlap) * 0.5;
-        dp[0] = x + half * nx * radius;
-        dp[1] = y + half * ny * radius;
-        dp[2] = z + half * nz * radius;
-        mp[0] = x - half * nx * radius;
-        mp[1] = y - half * ny * radius;
-        mp[2] = z - half * nz * radius;
-        const double volume = mr[SR_vol] / 2.0;
-        radius = pow(3.0 * volume / (4.0 * ORC_PI), 1.0 / 3.0);
-        const double area = 4.0 * ORC_PI * radius * radius;
-        const double dadt = 2.0 * mr[SR_dvdt] / radius;
-        mr[SR_vol] = dr[SR_vol] = volume;
-        mr[SR_area] = dr[SR_area] = area;
-        mr[SR_dadt] = dr[SR_dadt] = dadt;
-        mr[SR_radius] = dr[SR_radius] = radius;
-        dr[SR_bond_scale] = 1.0;
-        di[SI_fuse_tip] = 0;
-        for (int j = 6; j < 9; ++j) {
-            mr[SR_first + j] = 0.5 * mr[SR_first + j];
-            dr[SR_first + j] = 0.5 * dr[SR_first + j];
+        if (!nnew[i]) continue;
+        orec_t m = OREC(i), d1 = OREC(n + k), d2 = OREC(n + k + (nnew[i] == 2 ? 1 : 0));
+        odraw_t u = {draws, &next, seed, m.id[0], m.id[1], 1};
+        for (int c = 0; c < nnew[i]; ++c) {  /* copyChildParameters */
+            orec_t *d = c ? &d2 : &d1;
+            for (int j = 0; j < nreals; ++j) d->r[j] = m.r[j];
+            for (int j = 0; j < nints; ++j) d->q[j] = m.q[j];
         }
-        did[0] = di[SI_id] = (int)(next_id + k);
-        did[1] = di[SI_cpu] = my_proc;
-        ++k;
+        const int id1 = (int)(next_id + k);
+        if (nnew[i] == 2) {
+            odivide_tip_in_two(sp, &m, &d1, &d2, &u, id1, my_proc, id1 + 1, my_proc);
+            d2.id[0] = id1 + 1;
+            d2.id[1] = my_proc;
+        } else {
+            if (m.q[SI_cell_type] == BMXG_YEAST) odivide_cell(sp, &m, &d1, &u);
+            else odivide_segment(sp, &m, &d1, &u, id1, my_proc);
+            d1.q[SI_id] = id1;
+            d1.q[SI_cpu] = my_proc;
+        }
+        d1.id[0] = id1;
+        d1.id[1] = my_proc;
+        k += nnew[i];
     }
-#undef REC
+#undef OREC
+    free(nnew);
     return BMXG_OK;
 }

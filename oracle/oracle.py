@@ -95,8 +95,8 @@ def reflib():
         L.ref_surface_force.restype = None
         L.ref_init_bonds.argtypes = [_P, _G, _S, _i64, _i32, _i8, C.c_double]
         L.ref_particle_exchange.argtypes = [_S, _i64, _i32, _i8, _G, _d, _d, C.c_double, _d]
-        L.ref_split_cells_aos.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(SplitParams), C.c_double,
-                                          C.c_double, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, _i64, _i64]
+        L.ref_split_cells_aos.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(SplitParams),
+                                          C.c_void_p, C.c_int64, C.c_int64, C.c_int32, _i64, _i64]
         _ref = L
     return _ref
 
@@ -298,12 +298,11 @@ def particle_exchange(geom, P, vol, conc, dt, xpar, pl=None, params=None, use_re
     return c.reshape(3, P.n)
 
 
-def split_cells(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, use_ref=False,
-                split_prob=0.1, split_len=0.0030):
-    """YEAST division on AoS records (numpy, abi.aos_dtype(34, 35), room for the
-    daughters), in place.  use_ref runs the reference's own split loop bodies
-    (draws only; split_prob / split_len feed its FUNGI branches).  Returns
-    (rc, number of divisions)."""
+def split_cells(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, use_ref=False, return_used=False):
+    """Cell division on AoS records (numpy, abi.aos_dtype(34, 35), room for the
+    new particles), in place.  use_ref runs the reference's own split loop
+    bodies (draw sequence only).  Returns (rc, number of new particles), and
+    the draws the reference took when return_used."""
     out = C.c_int64(0)
     ptr = records.ctypes.data_as(C.c_void_p)
     if draws is not None:
@@ -312,12 +311,12 @@ def split_cells(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, use_re
     nd = 0 if draws is None else draws.size
     if use_ref:
         used = C.c_int64(0)
-        rc = _quiet(lambda: reflib().ref_split_cells_aos(ptr, int(n), len(records), C.byref(sp), split_prob,
-                                                         split_len, dptr, nd, int(next_id), int(my_proc),
-                                                         C.byref(out), C.byref(used)))
-    else:
-        rc = lib().orc_split_cells_aos(C.byref(sp), ptr, int(n), len(records), 34, 35, dptr, nd,
-                                       int(seed) & (2**64 - 1), int(next_id), int(my_proc), C.byref(out))
+        rc = _quiet(lambda: reflib().ref_split_cells_aos(ptr, int(n), len(records), C.byref(sp), dptr, nd,
+                                                         int(next_id), int(my_proc), C.byref(out),
+                                                         C.byref(used)))
+        return (rc, out.value, used.value) if return_used else (rc, out.value)
+    rc = lib().orc_split_cells_aos(C.byref(sp), ptr, int(n), len(records), 34, 35, dptr, nd,
+                                   int(seed) & (2**64 - 1), int(next_id), int(my_proc), C.byref(out))
     return rc, out.value
 
 

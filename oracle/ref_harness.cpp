@@ -375,8 +375,8 @@ void ref_surface_force(const bmxg_params *prm, const bmxg_particles *p, int64_t 
 // order; the scan and the daughters' slots n + offset[i] as at :57-75.
 // Daughters past cap return BMXG_ERR_CAPACITY before any write.
 int ref_split_cells_aos(void *particles, int64_t n, int64_t cap, const bmxg_split_params *sp,
-                        double split_prob, double split_len, const double *draws, int64_t ndraws,
-                        int64_t next_id, int32_t my_proc, int64_t *num_split, int64_t *draws_used)
+                        const double *draws, int64_t ndraws, int64_t next_id, int32_t my_proc,
+                        int64_t *num_split, int64_t *draws_used)
 {
     if (!particles || !sp || !num_split || n < 0 || cap < n) return BMXG_ERR_ARG;
     using ParticleType = SplitParticle;
@@ -384,7 +384,8 @@ int ref_split_cells_aos(void *particles, int64_t n, int64_t cap, const bmxg_spli
     ParticleType *pstruct = static_cast<ParticleType *>(particles);
     const int np = (int)n;
     const Real l_max_vol = sp->max_vol, l_max_len = sp->max_len, l_max_rad = sp->max_rad;
-    const Real l_brnch_prob = sp->brnch_prob, l_split_prob = split_prob, l_overlap = sp->overlap;
+    const Real l_brnch_prob = sp->brnch_prob, l_split_prob = sp->split_prob, l_overlap = sp->overlap;
+    const Real split_len = sp->split_len;
     const int l_num_reals = sp->num_reals, l_num_ints = sp->num_ints;
     long drawn = 0;
     amrex::RandomEngine engine;

@@ -88,10 +88,11 @@ SPLIT_MAX_VOL = 5.0e-10  # SPECIES::max_vol of the size the yeast decks use (m^3
 
 def split_params(**kw):
     """bmxg_split_params of BMX's defaults: overlap 0.2, 3 species (9 reals
-    past first_data), no extra ints; FUNGI limits of bmx_chem_species_parms.cpp."""
+    past first_data), no extra ints; FUNGI limits, split probability and split
+    length of bmx_chem_species_parms.cpp; no side branching unless asked."""
     from boltzmannmfx_gb300.abi import SplitParams
     sp = SplitParams(max_vol=SPLIT_MAX_VOL, overlap=0.2, max_len=0.0035, max_rad=0.00025,
-                     brnch_prob=0.0, num_reals=9, num_ints=0)
+                     brnch_prob=0.0, split_prob=0.1, split_len=0.0030, num_reals=9, num_ints=0)
     for k, v in kw.items():
         setattr(sp, k, v)
     return sp
@@ -134,3 +135,29 @@ def split_records(n, cap, seed, frac_divide=0.3, frac_fungi=0.2):
 def split_expected_count(a, n, max_vol=SPLIT_MAX_VOL):
     from boltzmannmfx_gb300.abi import INT_IDX as I, REAL_IDX as R, YEAST
     return int(np.count_nonzero((a["idata"][:n, I["cell_type"]] == YEAST) & (a["rdata"][:n, R["vol"]] > max_vol)))
+
+
+def split_fungi_records(n, cap, seed, frac_yeast=0.25):
+    """Seeded AoS records of hyphal segments in every state checkSplit looks at:
+    tips (isolated, with one or two bonds) at and below the length and radius
+    limits, segments behind a tip (SECOND_1 / SECOND_2, one to three bonds),
+    interior segments, and YEAST cells mixed in; every other field seeded."""
+    from boltzmannmfx_gb300.abi import FUNGI, INT_IDX as I, REAL_IDX as R, YEAST
+    a = split_records(n, cap, seed, frac_divide=0.3, frac_fungi=0.0)
+    rng = np.random.default_rng(seed + 1000)
+    fungi = rng.random(n) >= frac_yeast
+    pos = rng.integers(0, 4, n)
+    nb = np.where(pos == 0, rng.integers(0, 3, n), np.where(pos == 3, 2, rng.integers(1, 4, n)))
+    L = np.where(rng.random(n) < 0.6, rng.uniform(0.0035, 0.0045, n), rng.uniform(0.0025, 0.0035, n))
+    rad = np.where(rng.random(n) < 0.7, rng.uniform(0.00025, 0.0003, n), rng.uniform(0.0002, 0.00025, n))
+    a["idata"][:n, I["cell_type"]] = np.where(fungi, FUNGI, YEAST)
+    sel = np.flatnonzero(fungi)
+    a["idata"][sel, I["position"]] = pos[sel]
+    a["idata"][sel, I["n_bnds"]] = nb[sel]
+    a["idata"][sel, 15] = rng.integers(1, 3, sel.size)          # site1
+    a["rdata"][sel, R["c_length"]] = L[sel]
+    a["rdata"][sel, R["radius"]] = rad[sel]
+    a["rdata"][sel, R["theta"]] = rng.uniform(0.05, np.pi - 0.05, sel.size)
+    a["rdata"][sel, R["phi"]] = rng.uniform(0.0, 2.0 * np.pi, sel.size)
+    a["rdata"][sel, R["vol"]] = np.pi * rad[sel] ** 2 * L[sel]
+    return a

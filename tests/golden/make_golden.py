@@ -29,6 +29,10 @@ Cases:
   split_cells    split_particles (bmx_split_particles.cpp:47-54, :90-159 +
                  checkSplit / setNewCell) on 96 AoS records, YEAST cells around
                  max_vol with FUNGI interior segments mixed in, seeded draws
+  split_fungi    the same on 160 hyphal segments in every state checkSplit
+                 looks at (tips, segments behind tips, isolated segments),
+                 YEAST cells mixed in: tip extension, two-way tip split, side
+                 branch, halving (setNewSegment, setNewSegments)
   fungi_network  the 410-segment hyphal network of the reference's checkpoint
                  exec/fungi/chk357900 (level 2, read with bmxg_read_checkpoint),
                  deck exec/fungi/input_fungi, 5 steps at the stable rod step
@@ -328,10 +332,26 @@ def split_cells():
     print("split_cells:", n, ns)
 
 
+def split_fungi():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from common import split_fungi_records, split_params
+    n, cap = 160, 480
+    a = split_fungi_records(n, cap, 47)
+    draws = np.random.default_rng(53).random(8 * n)
+    sp = split_params(brnch_prob=0.3, split_prob=0.5)
+    out = a.copy()
+    rc, ns, used = O.split_cells(out, n, sp, draws=draws, use_ref=True, return_used=True)
+    assert rc == 0 and ns > 0
+    np.savez_compressed(os.path.join(OUT, "split_fungi.npz"), in_rec=a, out_rec=out, draws=draws[:used],
+                        n=np.array(n), num_split=np.array(ns),
+                        params=np.array([sp.brnch_prob, sp.split_prob, sp.split_len]))
+    print("split_fungi:", n, ns, used)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.have_ref():
         sys.exit("reference harness not built (reference tree missing?)")
     for f in (sphere_plain, rods_small, mixed, half_bond, pair_test, wall_test, colonies_small, min_distance,
-              init_bonds, fungi_network, exchange, split_cells):
+              init_bonds, fungi_network, exchange, split_cells, split_fungi):
         f()

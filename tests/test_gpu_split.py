@@ -1,30 +1,36 @@
-"""YEAST division through bmxg_split_cells_aos (host and device records)
-against the oracle and the golden vectors of the reference's split loop.
+"""Cell division through bmxg_split_cells_aos (host and device records) against
+the oracle and the golden vectors of the reference's split loop.
 
-Tolerance: every copied, halved or assigned field is bit-exact.  The fields
-that go through acos, sin, cos and pow (positions, radius, area, dadt) take
-CUDA's double-precision functions on the device and the C library's on the
-host; both are within 2 ulp of the true value, so they agree within
-8 x 2^-52 relative (positions: relative to |x| + r)."""
+Tolerance: every integer field and every real that the division copies,
+halves, adds or takes a square root of is bit-exact.  Reals that go through
+acos, sin, cos or pow (positions, the new segments' theta and phi, a YEAST
+cell's radius, area and dadt) take CUDA's double-precision functions on the
+device and the C library's on the host, each within 2 ulp of the true value;
+they agree within 64 x 2^-52 of the field's scale (positions: |x| plus the
+largest segment length or radius).  A new segment's angles are the
+reference's acos(z) and acos(x / sin theta), whose condition number is
+1 / |sin| of the result: a last-bit difference of the argument moves an angle
+near 0 or pi by that factor, so angles agree within
+128 x 2^-52 x (1 + 1 / |sin angle|)."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 from boltzmannmfx_gb300 import runtime
-from boltzmannmfx_gb300.abi import (BMXG_DEVICE, BMXG_ERR_ARG, BMXG_ERR_CAPACITY, BMXG_ERR_UNSUPPORTED,
-                                    BMXG_HOST, FUNGI, INT_IDX as I, REAL_IDX as R)
+from boltzmannmfx_gb300.abi import BMXG_DEVICE, BMXG_ERR_ARG, BMXG_ERR_CAPACITY, BMXG_HOST, REAL_IDX as R
 from boltzmannmfx_gb300.runtime import BmxgError
-from common import load, split_expected_count, split_params, split_records
+from common import load, split_expected_count, split_fungi_records, split_params, split_records
 
 pytestmark = pytest.mark.gpu
 
 EPS = 2.0 ** -52
-TRIG_REALS = (R["radius"], R["area"], R["dadt"])
+TRIG_REALS = (R["radius"], R["theta"], R["phi"], R["area"], R["vol"], R["dadt"])
 
 
 def assert_same_division(got, ref, n_used):
-    """bit-exact outside the transcendental fields, 8 ulp inside them"""
+    """ints bit-exact; reals bit-exact outside the transcendental fields,
+    64 ulp of the field's scale inside them; most of those bit-exact too"""
     g, r = got[:n_used], ref[:n_used]
     for f in ("id", "cpu", "idata"):
         assert np.array_equal(g[f], r[f]), f
@@ -32,16 +38,24 @@ def assert_same_division(got, ref, n_used):
     assert np.array_equal(g["rdata"][:, exact], r["rdata"][:, exact])
     for j in TRIG_REALS:
         a, b = g["rdata"][:, j], r["rdata"][:, j]
-        assert np.all(np.abs(a - b) <= 8 * EPS * np.abs(b)), j
-    scale = np.abs(r["pos"]) + np.abs(r["rdata"][:, R["radius"]])[:, None]
-    assert np.all(np.abs(g["pos"] - r["pos"]) <= 8 * EPS * scale)
+        if j in (R["theta"], R["phi"]):
+            tol = 128 * EPS * (1.0 + 1.0 / np.maximum(np.abs(np.sin(b)), 1e-6))
+        else:
+            tol = 64 * EPS * np.abs(b)
+        assert np.all(np.abs(a - b) <= tol), j
+    size = max(np.abs(r["rdata"][:, R["c_length"]]).max(), np.abs(r["rdata"][:, R["radius"]]).max())
+    assert np.all(np.abs(g["pos"] - r["pos"]) <= 64 * EPS * (np.abs(r["pos"]) + size))
     assert got[n_used:].tobytes() == ref[n_used:].tobytes()
+    same = np.mean(g["pos"] == r["pos"])
+    assert same > 0.5, same  # a last-bit difference of the trig functions is the exception
 
 
-def test_golden_host_records(gpu_lib):
-    d = load("split_cells")
+@pytest.mark.parametrize("case", ["split_cells", "split_fungi"])
+def test_golden_host_records(gpu_lib, case):
+    d = load(case)
     a = d["in_rec"].copy()
-    k = runtime.split_cells_aos(a, int(d["n"]), split_params(), draws=d["draws"])
+    kw = {} if case == "split_cells" else dict(brnch_prob=float(d["params"][0]), split_prob=float(d["params"][1]))
+    k = runtime.split_cells_aos(a, int(d["n"]), split_params(**kw), draws=d["draws"])
     assert k == int(d["num_split"])
     assert_same_division(a, d["out_rec"], int(d["n"]) + k)
 
@@ -59,37 +73,51 @@ def test_host_records_match_oracle(gpu_lib, oracle_lib, n, seed, frac):
     assert_same_division(a, b, n + k)
 
 
-def test_device_records_and_seeded_draws(gpu_lib, oracle_lib):
+@pytest.mark.parametrize("n,seed,bp,sprob", [(400, 1, 0.3, 0.5), (50_000, 2, 0.05, 0.1), (257, 3, 1.0, 0.0)])
+def test_fungi_records_match_oracle(gpu_lib, oracle_lib, n, seed, bp, sprob):
+    a = split_fungi_records(n, 3 * n, seed)
+    b = a.copy()
+    sp = split_params(brnch_prob=bp, split_prob=sprob)
+    draws = np.random.default_rng(seed + 10).random(8 * n)
+    got = runtime.split_cells_aos(a, n, sp, draws=draws, next_id=5, my_proc=1)
+    rc, want = oracle_lib.split_cells(b, n, sp, draws=draws, next_id=5, my_proc=1)
+    assert rc == 0 and got == want > 0
+    assert_same_division(a, b, n + got)
+
+
+@pytest.mark.parametrize("fungi", [False, True])
+def test_device_records_and_seeded_draws(gpu_lib, oracle_lib, fungi):
     import torch
     n = 50_000
-    a = split_records(n, n + n // 2, 13)
+    a = split_fungi_records(n, 3 * n, 13) if fungi else split_records(n, n + n // 2, 13)
     b = a.copy()
     seed = 0x5EED_0000_0000_0042
+    sp = split_params(brnch_prob=0.2, split_prob=0.5)
     dev = torch.from_numpy(a.view(np.uint8)).cuda()
-    k = runtime.split_cells_aos(dev.data_ptr(), n, split_params(), seed=seed, next_id=1 << 20, my_proc=1,
+    k = runtime.split_cells_aos(dev.data_ptr(), n, sp, seed=seed, next_id=1 << 20, my_proc=1,
                                 where=BMXG_DEVICE, cap=len(a))
     torch.cuda.synchronize()
     got = dev.cpu().numpy().view(a.dtype)
-    rc, want = oracle_lib.split_cells(b, n, split_params(), seed=seed, next_id=1 << 20, my_proc=1)
-    assert rc == 0 and k == want == split_expected_count(a, n)
+    rc, want = oracle_lib.split_cells(b, n, sp, seed=seed, next_id=1 << 20, my_proc=1)
+    assert rc == 0 and k == want > 0
     assert_same_division(got, b, n + k)
 
 
 def test_device_draws(gpu_lib, oracle_lib):
     import torch
     n = 20_000
-    a = split_records(n, 2 * n, 17)
+    a = split_fungi_records(n, 3 * n, 17)
     b = a.copy()
-    k = split_expected_count(a, n)
-    draws = np.random.default_rng(18).random(2 * k)
+    sp = split_params(brnch_prob=0.2, split_prob=0.5)
+    draws = np.random.default_rng(18).random(8 * n)
     dev = torch.from_numpy(a.view(np.uint8)).cuda()
     ddr = torch.from_numpy(draws).cuda()
-    got_k = runtime.split_cells_aos(dev.data_ptr(), n, split_params(), draws=(ddr.data_ptr(), ddr.numel()),
+    got_k = runtime.split_cells_aos(dev.data_ptr(), n, sp, draws=(ddr.data_ptr(), ddr.numel()),
                                     where=BMXG_DEVICE, cap=len(a))
     torch.cuda.synchronize()
-    rc, want = oracle_lib.split_cells(b, n, split_params(), draws=draws)
-    assert rc == 0 and got_k == want == k
-    assert_same_division(dev.cpu().numpy().view(a.dtype), b, n + k)
+    rc, want = oracle_lib.split_cells(b, n, sp, draws=draws)
+    assert rc == 0 and got_k == want > 0
+    assert_same_division(dev.cpu().numpy().view(a.dtype), b, n + got_k)
 
 
 def test_full_size_division(gpu_lib, oracle_lib):
@@ -110,20 +138,32 @@ def test_full_size_division(gpu_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("where", [BMXG_HOST, BMXG_DEVICE])
-def test_errors_write_nothing(gpu_lib, where):
+def test_errors_write_nothing(gpu_lib, oracle_lib, where):
     import torch
     n = 3000
-    a = split_records(n, 2 * n, 41)
-    k = split_expected_count(a, n)
-    draws = np.random.default_rng(42).random(2 * k)
+    a = split_fungi_records(n, 3 * n, 41)
+    sp = split_params(brnch_prob=0.2, split_prob=0.5)
+    full = np.random.default_rng(42).random(8 * n)
+    rc, k = oracle_lib.split_cells(a.copy(), n, sp, draws=full)
+    assert rc == 0 and k > 0
 
-    def call(rec, sp=None, dr=draws, cap=None):
+    def used_draws():
+        for m in range(0, 8 * n + 1, 64):  # the shortest prefix the oracle accepts
+            if oracle_lib.split_cells(a.copy(), n, sp, draws=full[:m])[0] == 0:
+                return m
+        return None
+
+    m = used_draws()
+    while oracle_lib.split_cells(a.copy(), n, sp, draws=full[:m - 1])[0] == 0:
+        m -= 1
+
+    def call(rec, dr, cap=None):
         if where == BMXG_HOST:
-            return runtime.split_cells_aos(rec, n, sp or split_params(), draws=dr, cap=cap)
+            return runtime.split_cells_aos(rec, n, sp, draws=dr, cap=cap)
         dev = torch.from_numpy(rec.view(np.uint8)).cuda()
         ddr = torch.from_numpy(np.ascontiguousarray(dr)).cuda()
         try:
-            return runtime.split_cells_aos(dev.data_ptr(), n, sp or split_params(), draws=(ddr.data_ptr(), len(dr)),
+            return runtime.split_cells_aos(dev.data_ptr(), n, sp, draws=(ddr.data_ptr(), len(dr)),
                                            where=BMXG_DEVICE, cap=len(rec) if cap is None else cap)
         finally:
             torch.cuda.synchronize()
@@ -131,20 +171,12 @@ def test_errors_write_nothing(gpu_lib, where):
 
     before = a.tobytes()
     with pytest.raises(BmxgError) as e:
-        call(a, cap=n + k - 1)
+        call(a, full, cap=n + k - 1)
     assert e.value.code == BMXG_ERR_CAPACITY and a.tobytes() == before
     with pytest.raises(BmxgError) as e:
-        call(a, dr=draws[:-1])
+        call(a, full[:m - 1])
     assert e.value.code == BMXG_ERR_ARG and a.tobytes() == before
-    t = a.copy()
-    t["idata"][5, I["cell_type"]] = FUNGI
-    t["idata"][5, I["position"]] = 1
-    tb = t.tobytes()
-    with pytest.raises(BmxgError) as e:
-        call(t, sp=split_params(brnch_prob=1e-4))
-    assert e.value.code == BMXG_ERR_UNSUPPORTED and t.tobytes() == tb
-    assert call(t, sp=split_params(brnch_prob=0.0)) == k - int(a["rdata"][5, R["vol"]] > 5.0e-10
-                                                                 and a["idata"][5, I["cell_type"]] == 0)
+    assert call(a, full[:m]) == k
 
 
 def test_empty_and_bad_layout(gpu_lib):

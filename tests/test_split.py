@@ -1,14 +1,14 @@
-"""YEAST division (split_particles) -- the oracle restatement against the
+"""Cell division (split_particles) -- the oracle restatement against the
 reference's own split loop bodies and against the committed golden vectors,
-and the call's error contract.  CPU only."""
+branch coverage of the FUNGI cases, and the call's error contract.  CPU only."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
-from boltzmannmfx_gb300.abi import (BMXG_ERR_ARG, BMXG_ERR_CAPACITY, BMXG_ERR_UNSUPPORTED, FUNGI,
-                                    INT_IDX as I, REAL_IDX as R, aos_dtype)
-from common import load, split_expected_count, split_params, split_records
+from boltzmannmfx_gb300.abi import (BMXG_ERR_ARG, BMXG_ERR_CAPACITY, FUNGI, YEAST, INT_IDX as I,
+                                    REAL_IDX as R, aos_dtype)
+from common import load, split_expected_count, split_fungi_records, split_params, split_records
 
 
 def test_aos_dtype_is_amrex_layout():
@@ -76,18 +76,88 @@ def test_division_properties(oracle_lib):
     assert np.array_equal(a["rdata"][kids][:, same], before["rdata"][div][:, same])
 
 
-def test_seeded_draws(oracle_lib):
+def seeded_sequence(O, a, n, sp, seed):
+    """The draw sequence that equals the seeded mode: each cell's checkSplit
+    draw is draw 0 of its (id, cpu) counter, its division's draws 1, 2, ..."""
+    checks = []
+    for i in range(n):
+        q, r = a["idata"][i], a["rdata"][i]
+        if q[I["cell_type"]] == FUNGI and ((q[I["position"]] == 0 and r[R["radius"]] >= sp.max_rad)
+                                           or q[I["position"]] in (1, 2)):
+            checks.append(O.split_uniform(seed, a["id"][i], a["cpu"][i], 0))
+    kinds, _ = decisions(a, n, sp, checks)
+    need = {"cell": 2, "tip": 2, "two": 4, "branch": 3, "halve": 0}
+    div = [O.split_uniform(seed, a["id"][i], a["cpu"][i], 1 + j) for i, k in kinds for j in range(need[k])]
+    return np.array(checks + div)
+
+
+@pytest.mark.parametrize("fungi", [False, True])
+def test_seeded_draws(oracle_lib, fungi):
     n = 500
-    a = split_records(n, 2 * n, 21)
+    a = split_fungi_records(n, 3 * n, 21) if fungi else split_records(n, 2 * n, 21)
     b = a.copy()
     seed = 0xB0A7_5EED_1234_5678
-    div = np.flatnonzero((a["idata"][:n, I["cell_type"]] == 0) & (a["rdata"][:n, R["vol"]] > 5.0e-10))
-    draws = np.array([[oracle_lib.split_uniform(seed, a["id"][i], a["cpu"][i], j) for j in (0, 1)]
-                      for i in div]).ravel()
+    sp = split_params(brnch_prob=0.3, split_prob=0.5)
+    draws = seeded_sequence(oracle_lib, a, n, sp, seed)
     assert np.all((draws >= 0.0) & (draws < 1.0))
-    rc1, k1 = oracle_lib.split_cells(a, n, split_params(), seed=seed)
-    rc2, k2 = oracle_lib.split_cells(b, n, split_params(), draws=draws)
-    assert rc1 == rc2 == 0 and k1 == k2 == len(div)
+    rc1, k1 = oracle_lib.split_cells(a, n, sp, seed=seed)
+    rc2, k2 = oracle_lib.split_cells(b, n, sp, draws=draws)
+    assert rc1 == rc2 == 0 and k1 == k2 > 0
+    assert a.tobytes() == b.tobytes()
+
+
+def decisions(a, n, sp, draws):
+    """checkSplit over the records with a draw sequence (bmx_chem_K.H:23-69),
+    restated here: the kind of each division and the draws the call takes."""
+    kinds, t = [], 0
+    for i in range(n):
+        q, r = a["idata"][i], a["rdata"][i]
+        if q[I["cell_type"]] == YEAST:
+            if r[R["vol"]] > sp.max_vol:
+                kinds.append((i, "cell"))
+            continue
+        pos, nb = q[I["position"]], q[I["n_bnds"]]
+        if pos == 0 and r[R["radius"]] >= sp.max_rad:
+            x = draws[t]
+            t += 1
+            if r[R["c_length"]] >= sp.max_len:
+                kinds.append((i, "halve" if nb == 0 else ("tip" if x > sp.split_prob else "two")))
+        elif pos in (1, 2):
+            x = draws[t]
+            t += 1
+            if x < sp.brnch_prob:
+                kinds.append((i, "halve" if nb == 0 else "branch"))
+    need = {"cell": 2, "tip": 2, "two": 4, "branch": 3, "halve": 0}
+    return kinds, t + sum(need[k] for _, k in kinds)
+
+
+def test_oracle_matches_golden_fungi(oracle_lib):
+    d = load("split_fungi")
+    a = d["in_rec"].copy()
+    sp = split_params(brnch_prob=float(d["params"][0]), split_prob=float(d["params"][1]))
+    rc, k = oracle_lib.split_cells(a, int(d["n"]), sp, draws=d["draws"])
+    assert rc == 0 and k == int(d["num_split"])
+    assert a.tobytes() == d["out_rec"].tobytes()
+    kinds, used = decisions(d["in_rec"], int(d["n"]), sp, d["draws"])
+    assert used == len(d["draws"])
+    assert {k for _, k in kinds} == {"cell", "tip", "two", "branch", "halve"}
+
+
+@pytest.mark.parametrize("n,seed,bp,sprob", [(400, 1, 0.3, 0.5), (3000, 2, 0.05, 0.1), (50, 3, 1.0, 0.0),
+                                             (1000, 4, 0.0, 1.0)])
+def test_oracle_matches_reference_fungi(oracle_lib, n, seed, bp, sprob):
+    oracle_lib.build(ref=None)
+    if not oracle_lib.have_ref():
+        pytest.skip("reference tree not present")
+    a = split_fungi_records(n, 4 * n, seed)
+    b = a.copy()
+    sp = split_params(brnch_prob=bp, split_prob=sprob)
+    kinds, need = decisions(a, n, sp, np.random.default_rng(seed + 10).random(8 * n))
+    draws = np.random.default_rng(seed + 10).random(8 * n)[:need]
+    rc2, k2, used = oracle_lib.split_cells(b, n, sp, draws=draws, use_ref=True, return_used=True)
+    rc1, k1 = oracle_lib.split_cells(a, n, sp, draws=draws)
+    assert rc1 == rc2 == 0 and k1 == k2 == sum(2 if k == "two" else 1 for _, k in kinds)
+    assert used == need
     assert a.tobytes() == b.tobytes()
 
 
@@ -103,24 +173,14 @@ def test_error_contract(oracle_lib):
     # too few draws
     rc, ns = oracle_lib.split_cells(a, n, split_params(), draws=draws[:-1])
     assert rc == BMXG_ERR_ARG and a.tobytes() == before
-    # a FUNGI tip at the length and radius limits, or a segment behind a tip
-    # that may branch: outside the YEAST division, refused before any write
-    t = a.copy()
-    t["idata"][0, I["cell_type"]] = FUNGI
-    t["idata"][0, I["position"]] = 0
-    t["rdata"][0, R["radius"]] = 0.00025
-    t["rdata"][0, R["c_length"]] = 0.0035
-    tb = t.tobytes()
-    rc, _ = oracle_lib.split_cells(t, n, split_params(), draws=draws)
-    assert rc == BMXG_ERR_UNSUPPORTED and t.tobytes() == tb
-    t["rdata"][0, R["c_length"]] = 0.0034
-    t["idata"][1, I["cell_type"]] = FUNGI
-    t["idata"][1, I["position"]] = 2
-    tb = t.tobytes()
-    rc, _ = oracle_lib.split_cells(t, n, split_params(brnch_prob=1e-4), draws=draws)
-    assert rc == BMXG_ERR_UNSUPPORTED and t.tobytes() == tb
-    rc, _ = oracle_lib.split_cells(t, n, split_params(brnch_prob=0.0), draws=draws)
-    assert rc == 0
+    f = split_fungi_records(300, 1200, 33)
+    fb = f.tobytes()
+    sp = split_params(brnch_prob=0.5, split_prob=0.5)
+    kinds, need = decisions(f, 300, sp, np.full(2400, 0.25))
+    rc, _ = oracle_lib.split_cells(f, 300, sp, draws=np.full(need - 1, 0.25))
+    assert rc == BMXG_ERR_ARG and f.tobytes() == fb
+    rc, ns = oracle_lib.split_cells(f, 300, sp, draws=np.full(need, 0.25))
+    assert rc == 0 and ns == sum(2 if k == "two" else 1 for _, k in kinds)
     # layout limits
     L = oracle_lib.lib()
     out = C.c_int64(0)
