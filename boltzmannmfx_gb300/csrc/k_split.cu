@@ -313,13 +313,16 @@ __device__ __forceinline__ void angles_of(double x, double y, double z, double &
 __device__ __forceinline__ void draw_around(double gst, double gct, double gphi, double u0, double u1,
                                             double &gnx, double &gny, double &gnz)
 {
-    const double gcp = cos(gphi), gsp = sin(gphi);
+    double gsp, gcp;
+    sincos(gphi, &gsp, &gcp);
     const double r00 = gcp * gst, r01 = -gsp, r02 = -gcp * gct;
     const double r10 = gsp * gst, r11 = gcp, r12 = -gsp * gct;
     const double r20 = gct, r21 = 0.0, r22 = gst;
     const double rtheta = 0.1 * u0;
     const double rphi = 2.0 * kPi * u1;
-    const double rct = cos(rtheta), rst = sin(rtheta), rcp = cos(rphi), rsp = sin(rphi);
+    double rst, rct, rsp, rcp;
+    sincos(rtheta, &rst, &rct);
+    sincos(rphi, &rsp, &rcp);
     const double rx = rct, ry = rst * rsp, rz = rst * rcp;
     gnx = r00 * rx + r01 * ry + r02 * rz;
     gny = r10 * rx + r11 * ry + r12 * rz;
@@ -469,7 +472,9 @@ __device__ void divide_segment(const SplitArgs &a, unsigned char *mrec, unsigned
         // zero gradient: +-45 degrees from phi in the xy plane
         const double da = u(0) > 0.5 ? 0.25 * kPi : -0.25 * kPi;
         const double tphi = phi + da;
-        const double gx = cos(tphi) / 1.0, gy = sin(tphi) / 1.0, gz = 0.0 / 1.0;
+        double stp, ctp;
+        sincos(tphi, &stp, &ctp);
+        const double gx = ctp / 1.0, gy = stp / 1.0, gz = 0.0 / 1.0;
         double gtheta, gst, gphi;
         angles_of(gx, gy, gz, gtheta, gst, gphi);
         double gnx, gny, gnz;
@@ -558,8 +563,10 @@ __device__ void divide_tip_in_two(const SplitArgs &a, unsigned char *mrec, unsig
     const double nx = st * cp, ny = st * sp, nz = ct;
     const double da = 0.25 * kPi;
     const double tphi1 = phi + da, tphi2 = phi - da;
-    const double gx1 = cos(tphi1), gy1 = sin(tphi1), gz1 = 0.0;
-    const double gx2 = cos(tphi2), gy2 = sin(tphi2), gz2 = 0.0;
+    double gy1, gx1, gy2, gx2;
+    sincos(tphi1, &gy1, &gx1);
+    sincos(tphi2, &gy2, &gx2);
+    const double gz1 = 0.0, gz2 = 0.0;
     double th, gst1, gphi1, gst2, gphi2;
     angles_of(gx1, gy1, gz1, th, gst1, gphi1);
     angles_of(gx2, gy2, gz2, th, gst2, gphi2);
