@@ -193,3 +193,34 @@ def test_empty_and_bad_layout(gpu_lib):
                                   None) == BMXG_ERR_ARG
     assert L.bmxg_split_cells_aos(C.byref(sp), p, 4, 3, 34, 35, None, 0, 0, 1, 0, BMXG_HOST, C.byref(out),
                                   None) == BMXG_ERR_ARG
+
+
+def test_other_layouts_match_oracle(gpu_lib, oracle_lib):
+    """records with more reals and ints than BMX's 34 / 35, and a species block
+    shorter than the increments the division halves (num_reals 3: the
+    daughter's first_data + 6..8 are not copied, and the reference halves what
+    the new record held), through the raw C ABI of both"""
+    from boltzmannmfx_gb300.abi import aos_dtype
+    n, cap, nreal, nint = 3000, 9000, 40, 40
+    src = split_fungi_records(n, cap, 61)
+    a = np.zeros(cap, aos_dtype(nreal, nint))
+    a["pos"] = src["pos"]
+    a["rdata"][:, :34] = src["rdata"]
+    a["rdata"][:, 34:] = np.random.default_rng(62).normal(size=(cap, 6))
+    a["id"], a["cpu"] = src["id"], src["cpu"]
+    a["idata"][:, :35] = src["idata"]
+    a["idata"][:, 35:] = 11
+    a0 = a
+    draws = np.random.default_rng(63).random(8 * n)
+    for sp in (split_params(brnch_prob=0.3, split_prob=0.5, num_reals=12, num_ints=3),
+               split_params(brnch_prob=0.3, split_prob=0.5, num_reals=3)):
+        a, b = a0.copy(), a0.copy()
+        out_g, out_o = C.c_int64(0), C.c_int64(0)
+        rc = gpu_lib.bmxg_split_cells_aos(C.byref(sp), a.ctypes.data_as(C.c_void_p), n, cap, nreal, nint,
+                                          draws.ctypes.data_as(C.c_void_p), draws.size, 0, 1, 0, BMXG_HOST,
+                                          C.byref(out_g), None)
+        ro = oracle_lib.lib().orc_split_cells_aos(C.byref(sp), b.ctypes.data_as(C.c_void_p), n, cap, nreal,
+                                                  nint, draws.ctypes.data_as(C.c_void_p), draws.size, 0, 1, 0,
+                                                  C.byref(out_o))
+        assert rc == ro == 0 and out_g.value == out_o.value > 0
+        assert_same_division(a, b, n + out_g.value)
