@@ -274,6 +274,30 @@ __global__ void k_pairs(const DevState S, const DevParams P, int a, int64_t *cnt
 // {YEAST, FUNGI}, whether any FUNGI segment is present, the largest radius
 // (non-negative doubles order as their bit patterns) and whether any radius
 // is NaN.  out: {bad, fungi, rmax bits, nan}, zeroed by the caller.
+// Whether a load repeats the device state bit for bit: each slot's position
+// (buffer a), radius and cell type against the caller's arrays at its caller
+// index.  *diff becomes nonzero on the first difference.
+__global__ void k_same_state(const DevState S, int a, const double *__restrict__ x, const double *__restrict__ y,
+                             const double *__restrict__ z, const double *__restrict__ r, const int *__restrict__ ct,
+                             unsigned long long *diff)
+{
+    unsigned d = 0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S.n; s += gridDim.x * blockDim.x) {
+        const int i = S.orig[s];
+        if ((unsigned)i >= (unsigned)S.n) {
+            d = 1u;
+            continue;
+        }
+        d |= (__double_as_longlong(x[i]) != __double_as_longlong(S.x[a][s])) ? 1u : 0u;
+        d |= (__double_as_longlong(y[i]) != __double_as_longlong(S.y[a][s])) ? 1u : 0u;
+        d |= (__double_as_longlong(z[i]) != __double_as_longlong(S.z[a][s])) ? 1u : 0u;
+        d |= (__double_as_longlong(r[i]) != __double_as_longlong(S.rad[s])) ? 1u : 0u;
+        d |= (ct[i] != (int)S.ctype[s]) ? 1u : 0u;
+    }
+    d = __reduce_or_sync(0xffffffffu, d);
+    if ((threadIdx.x & 31) == 0 && d) atomicOr(diff, 1ull);
+}
+
 __global__ void k_check_state(const int *__restrict__ ct, const double *__restrict__ r, int n,
                               unsigned long long *out)
 {
@@ -345,6 +369,13 @@ int launch_check_state(const int *ct, const double *r, int n, unsigned long long
                        cudaStream_t st)
 {
     k_check_state<<<grid, block, 0, st>>>(ct, r, n, out);
+    return 1;
+}
+
+int launch_same_state(const DevState &S, int a, const double *x, const double *y, const double *z, const double *r,
+                      const int *ct, unsigned long long *diff, int grid, int block, cudaStream_t st)
+{
+    k_same_state<<<grid, block, 0, st>>>(S, a, x, y, z, r, ct, diff);
     return 1;
 }
 
