@@ -293,13 +293,15 @@ def read_checkpoint(particles_dir, level=-1):
 
 def split_cells_aos(records, n, sp, draws=None, seed=0, next_id=1, my_proc=0, where=abi.BMXG_HOST,
                     nreal=34, nint=35, cap=None, stream=None):
-    """YEAST division (bmxg_split_cells_aos) on AoS records.
+    """Cell division (bmxg_split_cells_aos) on AoS records.
 
     where=BMXG_HOST: `records` is a numpy array of abi.aos_dtype(nreal, nint)
-    holding n particles and room for the daughters (len(records) = cap), and
-    `draws` a float64 numpy array or None.  where=BMXG_DEVICE: `records` and
-    `draws` are device addresses (ints, e.g. tensor.data_ptr()) and `cap` is
-    required.  Returns the number of divisions; raises BmxgError."""
+    holding n particles and room for the new ones (len(records) = cap), and
+    `draws` a float64 numpy array (the draw sequence) or None (the seeded
+    counter generator).  where=BMXG_DEVICE: `records` is a device address
+    (an int, e.g. tensor.data_ptr()), `draws` None or (device address, count),
+    and `cap` is required.  Returns the number of new particles; raises
+    BmxgError."""
     L = load_library()
     if where == abi.BMXG_HOST:
         if records.dtype != abi.aos_dtype(nreal, nint):

@@ -73,9 +73,10 @@ int  orc_particle_exchange(const bmxg_geometry *geom, const bmxg_particles *p, c
                            const int32_t *idx, const double *vol, double *conc, double dt,
                            const double xpar[3]);
 
-/* YEAST division of split_particles (bmx_split_particles.cpp:16-166,
- * checkSplit / copyChildParameters / setNewCell of bmx_chem_K.H:23-69,357-440)
- * on AoS records, with the contract of bmxg_split_cells_aos (host memory). */
+/* split_particles (bmx_split_particles.cpp:16-166, checkSplit /
+ * copyChildParameters / setNewCell / setNewSegment / setNewSegments of
+ * bmx_chem_K.H:23-69,357-1011,2129-2494) on AoS records, with the contract of
+ * bmxg_split_cells_aos (host memory). */
 int  orc_split_cells_aos(const bmxg_split_params *sp, void *particles, int64_t n, int64_t cap,
                          int32_t nreal, int32_t nint, const double *draws, int64_t ndraws,
                          uint64_t seed, int64_t next_id, int32_t my_proc, int64_t *num_split);

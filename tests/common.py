@@ -81,7 +81,7 @@ def within(a, b, rel, floor):
     return float(np.abs(a - b).max()) <= rel * float(np.abs(b).max()) + floor
 
 
-# YEAST division inputs -------------------------------------------------------
+# cell division inputs --------------------------------------------------------
 
 SPLIT_MAX_VOL = 5.0e-10  # SPECIES::max_vol of the size the yeast decks use (m^3)
 
