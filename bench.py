@@ -320,7 +320,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic, seeded (BASELINE configuration distributions)",
+            "data": "synthetic, seeded (the configurations' sizes and distributions)",
             "config": {"workload": w.name, "sample_particles": n, "sample_colonies": take},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
                              "sample": f"{take} colonies ({n} particles) per step, FP64, OpenMP"},
@@ -502,7 +502,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if prec == BMXG_FP32F else "f64",
-                "data": "synthetic, seeded (BASELINE configuration distributions)",
+                "data": "synthetic, seeded (the configurations' sizes and distributions)",
                 "config": {"workload": w.name, "particles": N, "colonies": w.ncol,
                            "form": "FP32F" if prec == BMXG_FP32F else "FP64",
                            "parallelism": f"replicas x{world}",
