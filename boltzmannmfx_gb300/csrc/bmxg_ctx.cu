@@ -960,7 +960,7 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
     cudaEvent_t k0, k1;
     prof_events(ctx, &k0, &k1);
     if (k0) cudaEventRecord(k0, st);
-    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, 256, st));
+    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, kListStepBlock, st));
     if (k1) cudaEventRecord(k1, st);
     return BMXG_OK;
 }

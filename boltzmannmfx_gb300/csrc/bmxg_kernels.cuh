@@ -47,6 +47,7 @@ constexpr int kNbrCap = 32;          // list entries per slot (more: the slot wa
 constexpr int kNbrInline = 3;        // entries held in the slot's list record beside its metadata
 constexpr int kNbrShift = 26;        // entry = slot | (bin shifts << 26)
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
+constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
 
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
 // by the step parity a (read) / b = a ^ 1 (write).
