@@ -48,6 +48,7 @@ constexpr int kNbrInline = 3;        // entries held in the slot's list record b
 constexpr int kNbrShift = 26;        // entry = slot | (bin shifts << 26)
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
 constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
+constexpr int kListBuildBlock = 128; // k_list_build's block (one slot per thread)
 
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
 // by the step parity a (read) / b = a ^ 1 (write).
