@@ -228,6 +228,23 @@ int grid_for(bmxg_ctx *ctx, const Shape &s, int64_t n)
     return (int)std::min<int64_t>(g, need);
 }
 
+// Launch shape of the per-slot stencil kernels (spheres, the differentiation
+// form): an autotuned shape when there is one; else one slot per thread in
+// 64-thread blocks.  The stencil walks differ in length from slot to slot, and
+// small blocks on a grid of every slot let the block scheduler balance them
+// (2.73 M spheres: FP64 6.66 -> 5.94 ms, FP32F 657 -> 600 us per step, against
+// 256-thread blocks striding over one wave).
+void stencil_shape(bmxg_ctx *ctx, const Shape &s, int64_t n, int *grid, int *block)
+{
+    if (s.grid > 0) {
+        *block = s.block;
+        *grid = grid_for(ctx, s, n);
+    } else {
+        *block = kSphereBlock;
+        *grid = (int)std::max<int64_t>(1, (n + kSphereBlock - 1) / kSphereBlock);
+    }
+}
+
 DevParams dev_params(const bmxg_params &p)
 {
     DevParams d{p.bndry_width, p.stiffness,     p.z_wall,      p.z_bndry_width, p.z_stiffness,
@@ -982,7 +999,9 @@ int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
     if (!S.has_rods) {
         const Shape &sh = ctx->sh_sphere[precision == BMXG_FP32F ? 1 : 0];
         if (k0) cudaEventRecord(k0, st);
-        LAUNCH(launch_sphere_step(S, P, dt, a, precision, grid_for(ctx, sh, n), sh.block, st, resync));
+        int sg, sb;
+        stencil_shape(ctx, sh, n, &sg, &sb);
+        LAUNCH(launch_sphere_step(S, P, dt, a, precision, sg, sb, st, resync));
         if (k1) cudaEventRecord(k1, st);
     } else {
         const int rg = grid_for(ctx, ctx->sh_rod, n);
@@ -1366,7 +1385,7 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
         Shape bs = ctx->sh_sphere[prec];
         const int blocks[] = {64, 128, 256};  // k_sphere is compiled with __launch_bounds__(256)
         for (int blk : blocks) {
-            for (int mult = 1; mult <= 16; mult *= 2) {
+            for (int mult = 1; mult <= 64; mult *= 2) {  // up to one slot per thread
                 Shape s;
                 s.block = blk;
                 s.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
@@ -1502,7 +1521,9 @@ int dfwd_step(bmxg_ctx *ctx, double dt)
     const int a = ctx->parity;
     const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, ctx->n);
     const Shape &sh = ctx->sh_sphere[0];
-    LAUNCH(launch_dfwd(S, dev_params(ctx->prm), diff_params(ctx), dt, a, grid_for(ctx, sh, ctx->n), sh.block,
+    int sg, sb;
+    stencil_shape(ctx, sh, ctx->n, &sg, &sb);
+    LAUNCH(launch_dfwd(S, dev_params(ctx->prm), diff_params(ctx), dt, a, sg, sb,
                        ctx->stream));
     LAUNCH(launch_rebuild(S, a ^ 1, ctx->scan_scratch, mgrd, mblk, ctx->stream));
     ctx->parity = a ^ 1;
@@ -1596,6 +1617,8 @@ int bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0, double *dL
     const DevParams P = dev_params(ctx->prm);
     const DiffParams D = diff_params(ctx);
     const Shape &sh = ctx->sh_sphere[0];
+    int ag, ab;
+    stencil_shape(ctx, sh, n, &ag, &ab);
     const int nseg = (T + K - 1) / K;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int c0 = seg * K, c1 = std::min(c0 + K, T);
@@ -1609,7 +1632,7 @@ int bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0, double *dL
         for (int t = c1 - 1; t >= c0; --t) {
             if ((rc = load_pos(ctx, ctx->segbuf + (size_t)(t - c0) * 3 * n))) return rc;
             LAUNCH(launch_dadj(S, P, D, ctx->traj_dt, 0, ctx->lam[cur], ctx->lam[cur ^ 1], ctx->gacc, ctx->gadh,
-                               grid_for(ctx, sh, n), sh.block, st));
+                               ag, ab, st));
             cur ^= 1;
         }
     }

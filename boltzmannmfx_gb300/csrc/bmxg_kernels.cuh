@@ -49,6 +49,7 @@ constexpr int kNbrShift = 26;        // entry = slot | (bin shifts << 26)
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
 constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
 constexpr int kListBuildBlock = 128; // k_list_build's block (one slot per thread)
+constexpr int kSphereBlock = 64;     // per-step sphere kernels' block (one slot per thread)
 
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
 // by the step parity a (read) / b = a ^ 1 (write).
