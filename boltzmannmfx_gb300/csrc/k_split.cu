@@ -26,8 +26,9 @@
 //                   the divisions;
 //   k_split_scan    exclusive scans of the block sums (one 1024-thread block
 //                   per array);
-//   k_split_index   the list of divisions in array order with their daughter
-//                   and draw offsets (block-local scans on the block offsets);
+//   k_split_index   the list of divisions with their daughter and draw
+//                   offsets (block-local scans on the block offsets), grouped
+//                   by kind of division;
 //   k_split_divide  one thread per division: the warp copies its mothers'
 //                   copied blocks into the daughters in coalesced rows, then
 //                   each lane runs its division.
@@ -77,8 +78,14 @@ struct SplitArgs {
     long long *cnt_n;     // [nb + 1] new particles
     long long *cnt_d;     // [nb + 1] division draws
     long long *cnt_k;     // [nb + 1] divisions
-    unsigned char *dec;   // [n] new particles | division draws << 2
+    unsigned char *dec;   // [n] new particles | division draws << 2 | kind << 5
+    int *kinds;           // [16]: divisions of each kind, then the fill counters of their regions
 };
+
+// kinds of division; the division list is grouped by kind so that a warp of
+// k_split_divide runs one kind's code (the list order does not change the
+// result: every entry carries its own daughter and draw offsets)
+enum { kCell = 0, kTip = 1, kBranch = 2, kTwo = 3, kHalve = 4, kKinds = 5 };
 
 struct Division {  // one entry of the division list
     int i;         // the mother
@@ -117,23 +124,24 @@ __device__ __forceinline__ int needs_check_draw(const SplitArgs &a, unsigned cha
 
 // checkSplit's decision (bmx_chem_K.H:23-69) given its draw x, and the number
 // of draws the division then takes (setNewCell 2; setNewSegment: isolated 0,
-// tip 2, side branch 3; setNewSegments 4), packed as n_new | draws << 2
+// tip 2, side branch 3; setNewSegments 4), packed as n_new | draws << 2 |
+// kind << 5
 __device__ __forceinline__ int decide(const SplitArgs &a, unsigned char *rec, double x)
 {
     const int *q = rec_i(a, rec);
     const double *r = rec_r(a, rec);
     const int ct = q[I_cell_type];
     const double vol = r[R_vol];  // issued with cell_type: another line of the record
-    if (ct == BMXG_YEAST) return vol > a.max_vol ? (1 | (2 << 2)) : 0;
+    if (ct == BMXG_YEAST) return vol > a.max_vol ? (1 | (2 << 2) | (kCell << 5)) : 0;
     if (ct != BMXG_FUNGI) return 0;
     const int pos = q[I_position], nb = q[I_n_bnds];
     if (pos == BMXG_SITE_TIP) {
         if (!(r[R_radius] >= a.max_rad) || !(r[R_c_length] >= a.max_len)) return 0;
-        if (x > a.split_prob || nb == 0) return 1 | ((nb == 0 ? 0 : 2) << 2);
-        return 2 | (4 << 2);
+        if (x > a.split_prob || nb == 0) return nb == 0 ? (1 | (kHalve << 5)) : (1 | (2 << 2) | (kTip << 5));
+        return 2 | (4 << 2) | (kTwo << 5);
     }
     if (pos == BMXG_SITE_SECOND_1 || pos == BMXG_SITE_SECOND_2)
-        return (x < a.brnch_prob) ? (1 | ((nb == 0 ? 0 : 3) << 2)) : 0;
+        return (x < a.brnch_prob) ? (nb == 0 ? (1 | (kHalve << 5)) : (1 | (3 << 2) | (kBranch << 5))) : 0;
     return 0;
 }
 
@@ -171,6 +179,9 @@ __global__ void __launch_bounds__(kBlock) k_split_checks(SplitArgs a)
 __global__ void __launch_bounds__(kBlock) k_split_decide(SplitArgs a)
 {
     __shared__ int ws[kBlock / 32];
+    __shared__ int sk[kKinds];
+    if (threadIdx.x < kKinds) sk[threadIdx.x] = 0;
+    __syncthreads();  // the counters are zero before any warp adds to them
     const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
     unsigned char *rec = a.par + (i < a.n ? i : 0) * a.stride;
     const int c = i < a.n ? needs_check_draw(a, rec) : 0;
@@ -185,15 +196,21 @@ __global__ void __launch_bounds__(kBlock) k_split_decide(SplitArgs a)
     }
     const int d = i < a.n ? decide(a, rec, x) : 0;
     if (i < a.n) a.dec[i] = (unsigned char)d;
+    // divisions of each kind: per warp into the block's counters, then one
+    // global atomic per kind and block (the block_excl barriers below order them)
+    const int kind = (d & 3) ? (d >> 5) : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, kind);
+    if (kind >= 0 && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&sk[kind], __popc(same));
     int tn, td, tk;
     block_excl(d & 3, ws, &tn);
-    block_excl(d >> 2, ws, &td);
+    block_excl((d >> 2) & 7, ws, &td);
     block_excl((d & 3) ? 1 : 0, ws, &tk);
     if (threadIdx.x == 0) {
         a.cnt_n[blockIdx.x] = tn;
         a.cnt_d[blockIdx.x] = td;
         a.cnt_k[blockIdx.x] = tk;
     }
+    if (threadIdx.x < kKinds && sk[threadIdx.x]) atomicAdd(&a.kinds[threadIdx.x], sk[threadIdx.x]);
 }
 
 // exclusive scan of c[0, nb) in place, total in c[nb]; block b scans array b
@@ -224,23 +241,39 @@ __global__ void __launch_bounds__(kScanThreads) k_split_scan(long long *c0, long
     if (t == kScanThreads - 1) c[nb] = s[t];
 }
 
-// the divisions in array order, with their daughters' and draws' offsets
+// the divisions with their daughters' and draws' offsets (from the array-order
+// scans), grouped by kind: the kinds' regions follow each other in kind order,
+// and within a region the entries land in arrival order
 __global__ void __launch_bounds__(kBlock) k_split_index(SplitArgs a, Division *list, long long checks)
 {
     __shared__ int ws[kBlock / 32];
+    __shared__ int sk[kKinds], sb[kKinds];
+    if (threadIdx.x < kKinds) sk[threadIdx.x] = 0;
     const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
     const int d = i < a.n ? a.dec[i] : 0;
     int t;
     const int on = block_excl(d & 3, ws, &t);
-    const int od = block_excl(d >> 2, ws, &t);
-    const int ok = block_excl((d & 3) ? 1 : 0, ws, &t);
-    if (!(d & 3)) return;
+    const int od = block_excl((d >> 2) & 7, ws, &t);
+    // a slot in the kind's region: the warp's share of the block's, the
+    // block's share of the region's (one global atomic per kind and block)
+    const int kind = (d & 3) ? (d >> 5) : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, kind);
+    const int lane = threadIdx.x & 31, lead = __ffs(same) - 1;
+    int slot = 0;
+    if (kind >= 0 && lane == lead) slot = atomicAdd(&sk[kind], __popc(same));
+    slot = __shfl_sync(0xffffffffu, slot, lead) + __popc(same & ((1u << lane) - 1u));
+    __syncthreads();
+    if (threadIdx.x < kKinds) sb[threadIdx.x] = sk[threadIdx.x] ? atomicAdd(&a.kinds[kKinds + threadIdx.x], sk[threadIdx.x]) : 0;
+    __syncthreads();
+    if (kind < 0) return;
+    int base = sb[kind];
+    for (int k = 0; k < kind; ++k) base += a.kinds[k];
     Division e;
     e.i = (int)i;
     e.kid = (int)(a.cnt_n[blockIdx.x] + on);
     e.draw = (int)(checks + a.cnt_d[blockIdx.x] + od);
     e.n_new = d & 3;
-    list[a.cnt_k[blockIdx.x] + ok] = e;
+    list[base + slot] = e;
 }
 
 // draw j of a division: from the sequence, or the counter generator (j + 1)
@@ -860,9 +893,10 @@ extern "C" int bmxg_split_cells_aos(const bmxg_split_params *sp, void *particles
     DevScratch &S = g_scratch[dev];
     std::lock_guard<std::mutex> lock(S.mu);
     const long long nb = (n + kBlock - 1) / kBlock;
-    // four block-sum arrays [nb + 1], the decisions [n], the list [n]
+    // four block-sum arrays [nb + 1], the kind counters, the decisions [n], the list [n]
     const size_t sums = align256(sizeof(long long) * (size_t)(nb + 1));
-    const size_t off_dec = 4 * sums;
+    const size_t off_kinds = 4 * sums;
+    const size_t off_dec = off_kinds + 256;
     const size_t off_list = align256(off_dec + (size_t)n);
     const size_t need = off_list + sizeof(Division) * (size_t)n;
     if (!S.host) SPLIT_CK(cudaMallocHost((void **)&S.host, 4 * sizeof(long long)));
@@ -879,6 +913,7 @@ extern "C" int bmxg_split_cells_aos(const bmxg_split_params *sp, void *particles
     a.cnt_d = (long long *)(S.dev + 2 * sums);
     a.cnt_k = (long long *)(S.dev + 3 * sums);
     a.dec = S.dev + off_dec;
+    a.kinds = (int *)(S.dev + off_kinds);
     Division *list = (Division *)(S.dev + off_list);
 
     Staging stage(st);
@@ -911,6 +946,7 @@ extern "C" int bmxg_split_cells_aos(const bmxg_split_params *sp, void *particles
         checks = S.host[0];
         if (ndraws < checks) return BMXG_ERR_ARG;  // too short for checkSplit's own draws
     }
+    SPLIT_CK(cudaMemsetAsync(a.kinds, 0, 16 * sizeof(int), st));
     k_split_decide<<<(unsigned)nb, kBlock, 0, st>>>(a);
     k_split_scan<<<3, kScanThreads, 0, st>>>(a.cnt_n, a.cnt_d, a.cnt_k, (int)nb);
     SPLIT_CK(cudaGetLastError());
