@@ -186,7 +186,10 @@ def adjoint_cost(Context, configs, BMXG_FP64, nsteps=200, ckpt=20):
             "params": "positions, stiffness, damping, drag, per-particle adhesion",
             "forward_ms_per_step": f_ms / nsteps, "adjoint_ms_per_step": b_ms / nsteps,
             "plain_fp64_ms_per_step": p_ms / nsteps,
-            "adjoint_over_forward": b_ms / f_ms, "adjoint_over_plain_fp64": b_ms / p_ms}
+            "adjoint_over_forward": b_ms / f_ms, "adjoint_over_plain_fp64": b_ms / p_ms,
+            "bar": "adjoint <= 3x the forward step: adjoint_over_forward compares it with the forward it "
+                   "differentiates (bmxg_forward, the law with every extension on); adjoint_over_plain_fp64 "
+                   "with the plain FP64 step of the reference law"}
 
 
 def split_cost(n, seed, reps=10, frac=0.05, fungi=False):
@@ -260,9 +263,12 @@ def split_cost(n, seed, reps=10, frac=0.05, fungi=False):
         t0 = time.perf_counter()
         runtime.split_cells_aos(h, n, sp, seed=it, next_id=n + 1)
         host_s.append(time.perf_counter() - t0)
+    # the oracle on the draws of the last timed call (seed reps + 2), so that
+    # its count is the one the GPU line reports
+    last_seed = reps + 2
     h = a.copy()
     t0 = time.perf_counter()
-    rc, kc = O.split_cells(h, n, sp, seed=0, next_id=n + 1)
+    rc, kc = O.split_cells(h, n, sp, seed=last_seed, next_id=n + 1)
     cpu_s = time.perf_counter() - t0
     alg = 14 * n + 968 * k
     peak, _ = measured_peak()
@@ -273,33 +279,59 @@ def split_cost(n, seed, reps=10, frac=0.05, fungi=False):
             "frac_of_measured_hbm": (alg / (ms * 1e-3) / 1e9) / peak if peak else None,
             "host_records_ms": 1e3 * float(np.median(host_s)),
             "cpu_baseline": {"kind": "port", "cores": 1, "ms_per_call": 1e3 * cpu_s,
-                             "records_per_s": n / cpu_s, "rc": rc, "new_particles": kc}}
+                             "records_per_s": n / cpu_s, "rc": rc, "new_particles": kc,
+                             "seed": last_seed, "same_count_as_gpu": bool(kc == k)}}
+
+
+def sample_colonies(w, target):
+    """Colonies of the workload whose sizes follow its colony-size mix: every
+    k-th colony in order of size (stratified), k chosen so that the sample
+    holds about `target` particles; all colonies when target >= the total.
+    Returns (particles, geometries, offsets, colonies taken)."""
+    from boltzmannmfx_gb300.abi import Particles
+    sizes = np.diff(w.offsets)
+    ncol = len(sizes)
+    if target >= int(sizes.sum()):
+        return w.particles, list(w.geoms), np.asarray(w.offsets), ncol
+    order = np.argsort(sizes, kind="stable")
+    k = max(1, int(round(sizes.sum() / max(target, 1))))
+    pick = np.sort(order[k // 2::k])
+    parts = [w.particles.subset(int(w.offsets[c]), int(w.offsets[c + 1])) for c in pick]
+    P = Particles.concat(parts)
+    off = np.zeros(len(pick) + 1, np.int64)
+    off[1:] = np.cumsum(sizes[pick])
+    return P, [w.geoms[c] for c in pick], off, len(pick)
+
+
+def cpu_rate(w, nth):
+    """Particle-steps/s of the oracle on one step of a ~100 000-particle
+    stratified sample (calibration for the sample sizes below)."""
+    from oracle import oracle as O
+    P, g, off, _ = sample_colonies(w, 100_000)
+    t1 = O.time_evolve(w.params, g, off, P, w.dt, 1, nth)
+    return P.n / max(t1, 1e-9)
 
 
 def cpu_baseline(w, budget_s=12.0):
     """Oracle (OpenMP over particles, all host threads) on a bounded sample of
-    the workload: whole colonies until ~budget_s of CPU work."""
+    the workload: a stratified sample of colonies (the workload's colony-size
+    mix) and the steps that fill ~budget_s of CPU work."""
     from oracle import oracle as O
     O.build(ref=False)
     nth = os.cpu_count() or 1
-    sizes = np.diff(w.offsets)
-    # one step on a first slice to calibrate
-    take = 1
-    while take < len(sizes) and sizes[:take].sum() < 100_000:
-        take += 1
-    P = w.particles.subset(0, int(w.offsets[take]))
-    t1 = O.time_evolve(w.params, w.geoms[:take], w.offsets[:take + 1], P, w.dt, 1, nth)
-    rate = sizes[:take].sum() / max(t1, 1e-9)
-    steps = int(max(1, min(w.steps, budget_s * rate / max(sizes[:take].sum(), 1))))
-    P = w.particles.subset(0, int(w.offsets[take]))
-    t = O.time_evolve(w.params, w.geoms[:take], w.offsets[:take + 1], P, w.dt, steps, nth)
-    n = int(sizes[:take].sum())
-    return {"value": n * steps / t, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"{take} of {len(sizes)} colonies ({n} particles) x {steps} steps, FP64, "
-                      f"{t:.1f} s wall"}
+    rate = cpu_rate(w, nth)
+    P, g, off, take = sample_colonies(w, min(w.n, int(rate * budget_s / 20)))
+    steps = int(max(1, min(w.steps, budget_s * rate / max(P.n, 1))))
+    t = O.time_evolve(w.params, g, off, P, w.dt, steps, nth)
+    return {"value": P.n * steps / t, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{take} of {len(w.offsets) - 1} colonies, stratified by size ({P.n} particles, "
+                      f"{100.0 * P.n / w.n:.1f} % of the workload) x {steps} steps, FP64, {t:.1f} s wall"}
 
 
 def run_reference(args):
+    """The CPU restatement of the reference path with all host threads, on the
+    whole workload when warm-up + timed steps fit in ~150 s of CPU work, else
+    on a stratified sample of its colonies that does."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -307,23 +339,25 @@ def run_reference(args):
     from oracle import oracle as O
     O.build(ref=False)
     nth = os.cpu_count() or 1
-    sizes = np.diff(w.offsets)
-    take = 1
-    while take < len(sizes) and sizes[:take].sum() < 60_000:
-        take += 1
-    n = int(sizes[:take].sum())
-    P = w.particles.subset(0, int(w.offsets[take]))
-    g, off = w.geoms[:take], w.offsets[:take + 1]
+    rate = cpu_rate(w, nth)
+    target = int(rate * 150.0 / max(args.steps + args.warmup, 1))
+    P, g, off, take = sample_colonies(w, min(w.n, target))
+    n = P.n
     O.time_evolve(w.params, g, off, P, w.dt, args.warmup, nth)
     t = O.time_evolve(w.params, g, off, P, w.dt, args.steps, nth)
     v = n * args.steps / t
+    whole = n == w.n
+    sample = ("the whole workload" if whole else
+              f"{take} of {len(w.offsets) - 1} colonies, stratified by size ({n} particles, "
+              f"{100.0 * n / w.n:.1f} % of the workload)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic, seeded (the configurations' sizes and distributions)",
-            "config": {"workload": w.name, "sample_particles": n, "sample_colonies": take},
+            "config": {"workload": w.name, "particles": w.n, "sample_particles": n, "sample_colonies": take,
+                       "sampled_fraction": n / w.n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": f"{take} colonies ({n} particles) per step, FP64, OpenMP"},
+                             "sample": f"{sample} per step, FP64, OpenMP"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "CPU restatement of the reference path (oracle/bmx_oracle.c); the reference "
                     "itself needs AMReX and MPI, which are not available"}

@@ -2,12 +2,11 @@
 //
 // Who needs it: code that may not call cudaMalloc on the step's path.  An
 // AMReX application such as BMX hands all device memory out through its own
-// arenas (and would rather not see a library grab memory behind them), and a
-// host program that records the step inside somebody else's CUDA stream
-// capture may not allocate while the capture is open.  This entry point runs
-// the same kernels as bmxg_step (binning, counting sort, k_sphere<FP64>) on
-// arrays the caller owns, with the binning scratch taken from a fixed
-// file-scope device array instead of from cudaMalloc.
+// arenas, sized up front, and a library that grabs memory behind them can
+// make the arena's next allocation fail or fragment the device.  This entry
+// point runs the same kernels as bmxg_step (binning, counting sort,
+// k_sphere<FP64>) on arrays the caller owns, with the binning scratch taken
+// from a fixed file-scope device array instead of from cudaMalloc.
 //
 // The array below is a static __device__ object: every GPU that loads the
 // library holds it (kScratchBytes) until the process exits.  Its host-side
@@ -79,8 +78,11 @@ using namespace bmxg;
 extern "C" int bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *geom, int64_t n,
                                         const double *x, const double *y, const double *z,
                                         const double *radius, double *x_out, double *y_out, double *z_out,
-                                        double *vel_x, double *vel_y, double *vel_z, double dt, void *stream)
+                                        double *vel_x, double *vel_y, double *vel_z, double dt, void *stream,
+                                        int64_t *n_out_of_domain)
 {
+    (void)cudaGetLastError();  // a non-sticky error another library left on this thread is not ours
+    if (n_out_of_domain) *n_out_of_domain = 0;
     if (!params || !geom || n < 0) return BMXG_ERR_ARG;
     // sizes first: beyond the fixed scratch is BMXG_ERR_CAPACITY, whatever else is wrong
     if (n > kMaxN) return BMXG_ERR_CAPACITY;                      // more than 32768 particles
@@ -150,9 +152,10 @@ extern "C" int bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_ge
     int *scan = reinterpret_cast<int *>(base + kOffScan);
 
     // every call reuses the same scratch: clear what must start at zero
-    cudaMemcpyAsync(base + kOffGeom, &G, sizeof(G), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(base + kOffCnt, 0, sizeof(DevCounters), st);
-    cudaMemsetAsync(S.colcnt, 0, sizeof(int) * ncols, st);
+    if (cudaMemcpyAsync(base + kOffGeom, &G, sizeof(G), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(base + kOffCnt, 0, sizeof(DevCounters), st) != cudaSuccess ||
+        cudaMemsetAsync(S.colcnt, 0, sizeof(int) * ncols, st) != cudaSuccess)
+        return BMXG_ERR_CUDA;
     const int block = 256;
     const int grid = (int)std::min<int64_t>((n + block - 1) / block, 4096);
     k_iota<<<grid, block, 0, st>>>(S.orig, (int)n);
@@ -162,10 +165,13 @@ extern "C" int bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_ge
     launch_bin(S, 0, grid, block, st);
     launch_rebuild(S, 0, scan, grid, block, st);
     launch_sphere_step(S, P, dt / 1.0, 0, BMXG_FP64_FORM, grid, block, st);
+    if (cudaGetLastError() != cudaSuccess) return BMXG_ERR_CUDA;  // a launch failed
     DevCounters h;
     if (cudaMemcpyAsync(&h, base + kOffCnt, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess) return BMXG_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return BMXG_ERR_CUDA;
-    if (cudaGetLastError() != cudaSuccess) return BMXG_ERR_CUDA;
+    if (n_out_of_domain) *n_out_of_domain = (int64_t)h.out_of_domain;
+    // as bmxg_step: inconsistent counting-sort counts are an internal error
+    if (h.bad_index) return BMXG_ERR_STATE;
     if (h.nonfinite) return BMXG_ERR_NONFINITE;
     return BMXG_OK;
 }

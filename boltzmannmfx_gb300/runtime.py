@@ -84,7 +84,7 @@ def load_library(path=None):
     L.bmxg_io_last_error.argtypes = []
     L.bmxg_set_ext.argtypes = [vp, C.POINTER(Ext)]
     L.bmxg_sphere_step_noalloc.argtypes = [C.POINTER(Params), C.POINTER(Geometry), C.c_int64] + [vp] * 10 + \
-        [C.c_double, vp]
+        [C.c_double, vp, C.POINTER(C.c_int64)]
     L.bmxg_split_cells_aos.argtypes = [C.POINTER(SplitParams), vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
                                        vp, C.c_int64, C.c_uint64, C.c_int64, C.c_int32, C.c_int32,
                                        C.POINTER(C.c_int64), vp]

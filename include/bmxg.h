@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define BMXG_ABI_VERSION 1
+#define BMXG_ABI_VERSION 2
 
 /* status codes */
 #define BMXG_OK              0
@@ -261,9 +261,9 @@ int  bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0,
 /* One FP64 step of a sphere colony on caller-owned DEVICE arrays, without
  * any device allocation.  This entry point has no counterpart in the
  * reference; it exists for callers that may not call cudaMalloc on the
- * step's path -- an application that hands out all device memory through
- * its own arenas (as AMReX does), or a host program recording the step
- * into someone else's stream capture, where allocation is not allowed.
+ * step's path: an application that hands out all device memory through its
+ * own arenas, sized up front (as AMReX does), where a library allocating
+ * behind the arena can make the arena's next allocation fail.
  * Inputs x, y, z, radius (n each) and outputs x_out, y_out, z_out and
  * vel_x..vel_z (n each; may not alias the inputs) are device pointers in
  * the caller's order; all particles are spheres of one colony with geometry
@@ -272,17 +272,23 @@ int  bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0,
  * Limits: n <= 32768 and n_cell[0] * n_cell[1] <= 65536, else
  * BMXG_ERR_CAPACITY.  The binning scratch is one fixed device array of about
  * 2.4 MB that every GPU loading the library holds until the process exits.
- * The first call on a device looks up that array's address (make it before
- * any stream capture).  Every call reuses the array: calls that overlap on
- * the GPU (other streams, other host threads) race and must not be issued.
+ * The first call on a device looks up that array's address; make that first
+ * call before any stream capture.  Every call reuses the array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must not
+ * be issued.
  * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
- * returns after it completes. */
+ * returns after it completes.  *n_out_of_domain (may be NULL) receives the
+ * particles whose new z left the non-periodic range (kept, as bmxg_step
+ * keeps them and counts them in bmxg_stats.n_out_of_domain).  Returns
+ * BMXG_ERR_NONFINITE for a non-finite new position and BMXG_ERR_STATE when
+ * the counting sort's counts came out inconsistent (an internal error), as
+ * bmxg_step does. */
 int  bmxg_sphere_step_noalloc(const bmxg_params *params, const bmxg_geometry *geom,
                               int64_t n, const double *x, const double *y,
                               const double *z, const double *radius,
                               double *x_out, double *y_out, double *z_out,
                               double *vel_x, double *vel_y, double *vel_z,
-                              double dt, void *stream);
+                              double dt, void *stream, int64_t *n_out_of_domain);
 
 /* ---- start-up bonds ----------------------------------------------------- */
 

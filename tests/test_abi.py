@@ -33,7 +33,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_version(lib):
-    assert lib.bmxg_version() == 1
+    assert lib.bmxg_version() == 2
 
 
 def test_create_without_device_fails_cleanly(lib):

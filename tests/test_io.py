@@ -13,7 +13,7 @@ from boltzmannmfx_gb300.abi import BMXG_ERR_ARG, BMXG_ERR_UNSUPPORTED, FUNGI, Pa
 from boltzmannmfx_gb300.runtime import BmxgError, read_ascii, read_checkpoint, write_ascii, write_vtk
 from common import load
 
-REF = os.environ.get("BMX_REFERENCE", "/root/reference")
+from oracle.oracle import REF_TREE as REF  # noqa: E402  (BMX_REFERENCE, else the oracle recipe's default)
 CHK = os.path.join(REF, "exec/fungi/chk357900/particles")
 need_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "exec")), reason="reference tree not present")
 
