@@ -51,6 +51,9 @@ def parse():
                     choices=["colonies", "sphere_fp32", "sphere_plain", "rod_trees"])
     ap.add_argument("--precision", default=None, choices=[None, "fp32f", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--only-main", action="store_true",
+                    help="the timed steps and the roofline leg only (no other form, end-to-end, adjoint, "
+                         "division or CPU legs): the run profiles capture")
     ap.add_argument("--only-split", action="store_true",
                     help="print only the cell-division measurements (2 731 333 records, YEAST and FUNGI)")
     return ap.parse_args()
@@ -477,6 +480,18 @@ def run_ours(args):
             "frac": achieved / peak, "peak_kind": peak_kind, "kernel_ms": k_ms,
             "algorithmic_bytes_per_launch": alg,
             "traffic": ncu_traffic(f"{w.name}:{kname}")}
+
+    if args.only_main:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": ms / args.steps, "roofline": roof,
+                              "gpu_launches": int(launches), "list_builds": int(rebins),
+                              "note": "--only-main: a profiling run, not a bench line"}), flush=True)
+        ctx.close()
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
 
     # the other form on the same workload, and the FP32F force error against FP64
     other = BMXG_FP64 if prec == BMXG_FP32F else BMXG_FP32F
