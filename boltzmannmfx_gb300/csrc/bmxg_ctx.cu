@@ -109,6 +109,11 @@ struct bmxg_ctx {
     ListCtl *h_lctl = nullptr;    // pinned copy of the control block
     unsigned long long body_runs_seen = 0;  // list builds already counted as launches
     bool capturing = false;       // enqueue_step runs inside a graph capture
+    bool pair_capture = false;    // list steps record their gated pairs (S.pcap)
+    bool pcap_valid = false;      // S.pcap holds the last step's gated pairs
+    bool fx_ahead = false;        // list steps moved the fixed-point positions past the FP64 ones
+    std::vector<FxGeom> h_fxg;    // per colony fixed-point geometry of the list path
+    FxGeom *d_fxg = nullptr;
     cudaStream_t body_stream = nullptr;     // captures the bodies of conditional nodes
 
     // loads and stores of host arrays: the copies run on io_stream, overlapped
@@ -123,6 +128,8 @@ struct bmxg_ctx {
 };
 
 namespace {
+
+int sync_fp64(bmxg_ctx *ctx);
 
 int fail(bmxg_ctx *c, int code, const std::string &msg)
 {
@@ -216,6 +223,8 @@ void free_state(bmxg_ctx *ctx)
     ctx->uperm = nullptr;
     ctx->have_state = false;
     ctx->list_valid = false;
+    ctx->fx_ahead = false;
+    ctx->d_fxg = nullptr;
     ctx->bins_exact = true;
 }
 
@@ -294,6 +303,7 @@ int check_geom(const bmxg_geometry &g, std::string &why)
 void build_geoms(bmxg_ctx *ctx)
 {
     ctx->h_geoms.resize(ctx->ncol);
+    ctx->h_fxg.resize(ctx->ncol);
     int col_base = 0;
     int64_t cell_base = 0;
     for (int c = 0; c < ctx->ncol; ++c) {
@@ -331,6 +341,28 @@ void build_geoms(bmxg_ctx *ctx)
         // two bins apart at most per axis: |r|^2 < 4 (dx^2 + dy^2 + dz^2)
         G.nbh_trivial = (ctx->prm.neighborhood >= diag2 * (1.0 + 1e-9)) ? 1 : 0;
         G.invny = 1.0f / (float)G.n[1];
+        // 64-bit fixed point of the list path: a periodic axis spans the
+        // domain, a closed one four lengths from one length below plo
+        FxGeom &F = ctx->h_fxg[c];
+        std::memset(&F, 0, sizeof(F));
+        for (int d = 0; d < 3; ++d) {
+            const double span = G.per[d] ? G.len[d] : 4.0 * G.len[d];
+            F.o[d] = G.per[d] ? G.plo[d] : G.plo[d] - G.len[d];
+            F.u[d] = std::ldexp(span, -64);
+            F.uh[d] = (float)std::ldexp(span, -32);
+            const long double cx = std::ldexp(1.0L / (long double)span, 64);
+            F.c[d] = (float)cx;
+            F.cl[d] = (float)(cx - (long double)F.c[d]);
+            F.n[d] = G.n[d];
+            F.per[d] = G.per[d];
+            F.plo[d] = G.plo[d];
+            F.phi[d] = G.phi[d];
+        }
+        {
+            const long double t = ((long double)ctx->prm.z_wall - (long double)F.o[2]) / (long double)F.u[2];
+            const long double hi = std::floor(t / 4294967296.0L);
+            F.zw = (hi <= 0.0L) ? 0u : (hi >= 4294967295.0L ? 4294967295u : (unsigned)hi);
+        }
         // height of each z-bin's lower face above the growth surface, with the
         // same FP64 face the re-binning uses, split into a float pair
         G.nwz = std::min(G.n[2] + 2, kWallTable);
@@ -430,6 +462,7 @@ int bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params)
 {
     if (!ctx) return BMXG_ERR_ARG;
     if (check_params(params)) return fail(ctx, BMXG_ERR_ARG, "non-finite force parameter");
+    if (int rc = sync_fp64(ctx)) return rc;  // the list's fixed point restarts from the FP64 positions
     ctx->prm = *params;
     drop_graphs(ctx);
     ctx->list_valid = false;
@@ -437,6 +470,8 @@ int bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params)
         build_geoms(ctx);
         CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol,
                            cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_fxg, ctx->h_fxg.data(), sizeof(FxGeom) * ctx->ncol, cudaMemcpyHostToDevice,
+                           ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
     }
     return BMXG_OK;
@@ -517,6 +552,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
                                !p->split_flag && !p->new_flag && !p->dltd;
     if (n && only_required && ctx->have_state && ctx->n == n && ctx->offsets == off && !ctx->S.has_rods) {
         cudaStream_t st = ctx->stream;
+        if (int rc = sync_fp64(ctx)) return rc;
         if (join.s) CK(cudaStreamWaitEvent(st, ctx->io_ev[1], 0));  // staged positions
         CK(cudaMemsetAsync(ctx->d_chk, 0, sizeof(unsigned long long), st));
         LAUNCH(launch_same_state(ctx->S, ctx->parity, src_x, src_y, src_z, src_r, src_ct, ctx->d_chk,
@@ -531,6 +567,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
             CK(cudaStreamSynchronize(st));
             ctx->stepped = false;
             ctx->vel32 = false;
+            ctx->pcap_valid = false;
             ctx->d_adh = nullptr;
             free_adjoint(ctx);
             std::memset(&ctx->stats, 0, sizeof(ctx->stats));
@@ -587,6 +624,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     } while (0)
     if (!reuse) {
     AL(ctx->d_geoms, ctx->ncol);
+    AL(ctx->d_fxg, ctx->ncol);
     AL(ctx->d_cbase, ctx->ncol + 1);
     AL(ctx->d_cnt, 1);
     for (int k = 0; k < 2; ++k) {
@@ -610,12 +648,14 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     }  // !reuse
 #undef AL
     S.geoms = ctx->d_geoms;
+    S.fxg = ctx->d_fxg;
     S.cbase = ctx->d_cbase;
     S.cnt = ctx->d_cnt;
     cudaStream_t st = ctx->stream;
     if (!reuse) {  // same colonies as the loaded state: the device copies are current
         CK(cudaMemcpyAsync(ctx->d_geoms, ctx->h_geoms.data(), sizeof(DevGeom) * ctx->ncol, cudaMemcpyHostToDevice,
                            st));
+        CK(cudaMemcpyAsync(ctx->d_fxg, ctx->h_fxg.data(), sizeof(FxGeom) * ctx->ncol, cudaMemcpyHostToDevice, st));
         ctx->h_cbase.assign(off.begin(), off.end());
         CK(cudaMemcpyAsync(ctx->d_cbase, ctx->h_cbase.data(), sizeof(int) * (ctx->ncol + 1), cudaMemcpyHostToDevice,
                            st));
@@ -704,6 +744,8 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     ctx->parity = 0;
     ctx->rmax = rmax;
     ctx->list_valid = false;
+    ctx->pcap_valid = false;
+    ctx->fx_ahead = false;
     ctx->bins_exact = true;
     ctx->d_adh = nullptr;  // per-particle adhesion must be given again for the new state
     free_adjoint(ctx);
@@ -717,6 +759,7 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     if (!ctx) return BMXG_ERR_ARG;
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (int rc = sync_fp64(ctx)) return rc;
     if (!p || p->n != ctx->n) return fail(ctx, BMXG_ERR_ARG, "particle count differs from the loaded state");
     if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
     const int64_t n = ctx->n;
@@ -850,26 +893,28 @@ void prof_events(bmxg_ctx *ctx, cudaEvent_t *k0, cudaEvent_t *k1)
 }
 
 // ---- FP32F neighbour list with a skin ---------------------------------------
-constexpr int kListMaxAge = 64;      // bounds the FP32 drift of the frozen-frame offsets
-constexpr int kListExactEvery = 8;   // builds between exact FP64 re-binnings
+constexpr int kListMaxAge = 64;      // builds at least this often
 constexpr int kListMinSteps = 2;     // a shorter first call after a load runs the per-step path
 
 // Skin of the list for the loaded state and parameters, or 0 where the list
 // would not reproduce the reference's pair set: the largest cutoff
 // 2 r_max + bw plus the skin must stay within the smallest bin width (so
 // that every pair inside the cutoff is a stencil pair whatever the bins),
-// and BMXCheckPair must hold for every stencil pair.
+// BMXCheckPair must hold for every stencil pair, and the fixed point's high
+// word must resolve offsets to 2^-20 of a bin.
 float list_skin(const bmxg_ctx *ctx)
 {
     if (ctx->S.has_rods || ctx->n == 0 || ctx->n >= (1LL << kNbrShift)) return 0.0f;
     if (ctx->ncells_total >= (1LL << 30)) return 0.0f;  // 3D cell offsets of the build
     double skin = 1e300;
     for (const DevGeom &g : ctx->h_geoms) {
-        if (!g.nbh_trivial || g.n[2] > 0xffff) return 0.0f;
+        if (!g.nbh_trivial) return 0.0f;
         const double dmin = std::min(g.dx[0], std::min(g.dx[1], g.dx[2]));
         const double rcut = 2.0 * ctx->rmax + ctx->prm.bndry_width;
         const double sk = std::min(0.25 * dmin, 0.95 * (dmin - rcut));
         if (!(sk >= 0.02 * dmin)) return 0.0f;
+        for (int d = 0; d < 3; ++d)
+            if (!(std::ldexp((g.per[d] ? 1.0 : 4.0) * g.len[d], -32) <= std::ldexp(dmin, -20))) return 0.0f;
         skin = std::min(skin, sk);
     }
     return (float)skin;
@@ -884,6 +929,10 @@ int ensure_list(bmxg_ctx *ctx, float skin)
         int rc;
         if ((rc = dalloc(ctx, &S.nbr, (size_t)(kNbrCap - kNbrInline) * ctx->n))) return rc;
         if ((rc = dalloc(ctx, &S.lrec, ctx->n))) return rc;
+        for (int k = 0; k < 2; ++k) {
+            if ((rc = dalloc(ctx, &S.fxh[k], ctx->n))) return rc;
+            if ((rc = dalloc(ctx, &S.fxl[k], 3 * (size_t)ctx->n))) return rc;
+        }
         if ((rc = dalloc(ctx, &S.cellcnt, ctx->ncells_total))) return rc;
         if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
         if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints((int)ctx->ncells_total)))) return rc;
@@ -905,10 +954,10 @@ int ensure_list(bmxg_ctx *ctx, float skin)
         h.inc_max[k] = 0x007fffffu;
     }
     h.max_age = kListMaxAge;
-    // a state whose list bins (buffer kListBins) are the exact bins of its
-    // current positions needs no FP64 re-binning for the first build
-    h.force = (ctx->bins_exact && ctx->parity == kListBins) ? 2 : 1;
-    h.exact_every = kListExactEvery;
+    h.force = 1;
+    // the fixed-point positions start from the FP64 ones
+    LAUNCH(launch_list_init(S, ctx->parity, grid_for(ctx, ctx->sh_misc, ctx->n), ctx->sh_misc.block, ctx->stream));
+    ctx->fx_ahead = false;
     CK(cudaMemcpyAsync(S.lctl, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->skin_cur = skin;
@@ -919,8 +968,21 @@ int ensure_list(bmxg_ctx *ctx, float skin)
 
 // Bins of buffer `parity` as the reference has them (after list steps froze
 // them); every consumer of the bins other than a list step calls this.
+// FP64 positions of buffer `parity` from the list path's fixed point, when
+// list steps ran since they were last written; every reader of the FP64
+// positions calls this first.
+int sync_fp64(bmxg_ctx *ctx)
+{
+    if (!ctx->fx_ahead || !ctx->have_state || ctx->n == 0) return BMXG_OK;
+    LAUNCH(launch_list_to_fp64(ctx->S, ctx->parity, grid_for(ctx, ctx->sh_misc, ctx->n), ctx->sh_misc.block,
+                               ctx->stream));
+    ctx->fx_ahead = false;
+    return BMXG_OK;
+}
+
 int ensure_exact(bmxg_ctx *ctx)
 {
+    if (int rc = sync_fp64(ctx)) return rc;
     if (ctx->bins_exact || !ctx->have_state) return BMXG_OK;
     const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, ctx->n);
     LAUNCH(launch_bin(ctx->S, ctx->parity, grd, blk, ctx->stream));
@@ -1084,6 +1146,12 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     }
     if ((skin > 0.0f) != ctx->list_on) drop_graphs(ctx);
     ctx->list_on = skin > 0.0f;
+    ctx->pcap_valid = false;
+    if (ctx->list_on && ctx->pair_capture && !ctx->S.pcap) {
+        int rc = dalloc(ctx, &ctx->S.pcap, (size_t)(kPairCap + 1) * ctx->n);
+        if (rc) return rc;
+        drop_graphs(ctx);
+    }
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int32_t left = nsteps;
     ctx->kev_used = 0;
@@ -1131,6 +1199,7 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
         if (rc) return rc;
     }
     ctx->vel32 = (precision == BMXG_FP32F) && !ctx->S.has_rods;
+    ctx->pcap_valid = ctx->list_on && ctx->S.pcap != nullptr;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1138,6 +1207,7 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
         CK(cudaMemcpyAsync(ctx->h_lctl, ctx->S.lctl, sizeof(ListCtl), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (ctx->list_on) {
+        ctx->fx_ahead = true;
         const unsigned long long runs = ctx->h_lctl->body_runs - ctx->body_runs_seen;
         ctx->body_runs_seen = ctx->h_lctl->body_runs;
         ctx->launches += (int64_t)runs * kListBodyKernels;
@@ -1165,6 +1235,8 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     ctx->stats.n_bond_repairs = (int64_t)ctx->h_cnt->bond_repairs;
     if (ctx->h_cnt->bad_index) return fail(ctx, BMXG_ERR_STATE, "internal: inconsistent bin counts");
     if (ctx->h_cnt->nonfinite) return fail(ctx, BMXG_ERR_NONFINITE, "a step produced a non-finite position");
+    if (ctx->h_cnt->range)
+        return fail(ctx, BMXG_ERR_STATE, "a z left the FP32F list path's range (three quarters of a length past the domain)");
     return BMXG_OK;
 }
 
@@ -1194,6 +1266,49 @@ int bmxg_set_profiling(bmxg_ctx *ctx, int32_t on)
     if (ctx->profiling) {
         ctx->stats.main_kernel_ms = 0.0;
         ctx->stats.main_kernel_launches = 0;
+    }
+    return BMXG_OK;
+}
+
+int bmxg_set_pair_capture(bmxg_ctx *ctx, int32_t on)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if ((on != 0) != ctx->pair_capture) drop_graphs(ctx);  // captured steps hold S by value
+    ctx->pair_capture = on != 0;
+    if (!ctx->pair_capture) ctx->S.pcap = nullptr;  // the buffer stays with the state's allocations
+    ctx->pcap_valid = false;
+    return BMXG_OK;
+}
+
+int bmxg_get_step_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int64_t cap, int64_t *total)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();
+    if (!offs || !total) return fail(ctx, BMXG_ERR_ARG, "offs and total are required");
+    if (!ctx->pcap_valid || !ctx->S.pcap) return fail(ctx, BMXG_ERR_STATE, "no list step recorded with capture on");
+    const int64_t n = ctx->n;
+    const size_t w = kPairCap + 1;
+    std::vector<int> rec((size_t)n * w), orig((size_t)n);
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(rec.data(), ctx->S.pcap, sizeof(int) * rec.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(orig.data(), ctx->S.orig, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<int64_t> slot_of((size_t)n);
+    for (int64_t i = 0; i < n; ++i) slot_of[(size_t)orig[(size_t)i]] = i;
+    offs[0] = 0;
+    bool over = false;
+    for (int64_t o = 0; o < n; ++o) {
+        const int k = rec[(size_t)slot_of[(size_t)o] * w];
+        over |= k > kPairCap;
+        offs[o + 1] = offs[o] + std::min(k, kPairCap);
+    }
+    *total = offs[n];
+    if (over) return fail(ctx, BMXG_ERR_CAPACITY, "a particle had more gated pairs than the capture holds");
+    if (offs[n] > cap) return fail(ctx, BMXG_ERR_CAPACITY, "pair buffer too small");
+    if (!idx) return BMXG_OK;
+    for (int64_t o = 0; o < n; ++o) {
+        const int *r = &rec[(size_t)slot_of[(size_t)o] * w];
+        for (int k = 0; k < r[0]; ++k) idx[offs[o] + k] = orig[(size_t)r[1 + k]];
     }
     return BMXG_OK;
 }

@@ -57,6 +57,26 @@ struct DevGeom {
     float2 wz[kWallTable];
 };
 
+// 64-bit fixed-point positions of the FP32F list path (one record per colony):
+// per axis X = (x - o) / u with u = span / 2^64 and X in [0, 2^64).  A
+// periodic axis spans the domain (o = plo, span = len: the unsigned wrap of X
+// is the periodic wrap, and the int32 difference of two high words is the
+// minimum-image offset); a closed axis spans 4 lengths from one length below
+// plo, so the domain is the high word in [2^30, 2^31).
+struct alignas(16) FxGeom {
+    float uh[3];                // span / 2^32: the unit of the high word (pair offsets)
+    unsigned zw;                // high word of the growth surface z_wall (z axis)
+    float c[3];                 // 2^64 / span as an FP32 pair c + cl (an increment in units)
+    float pad0;
+    float cl[3];
+    float pad1;
+    int n[3];                   // bins per axis (the list build's cells)
+    int per[3];
+    int pad[2];
+    double o[3], u[3];          // origin and unit (FP64: conversions at the path's ends)
+    double plo[3], phi[3];      // the domain (clamp of converted periodic positions)
+};
+
 // Counters a step accumulates on the device.
 struct DevCounters {
     unsigned long long out_of_domain;
@@ -66,6 +86,7 @@ struct DevCounters {
     unsigned long long pairs;
     unsigned long long bond_repairs;
     unsigned long long moved;
+    unsigned long long range;      // list path: a z left the fixed-point range (sticky)
 };
 
 // Force parameters, fpar[0..8] (src/chemistry/bmx_cell_interaction.cpp:84-93).

@@ -33,11 +33,8 @@ struct ListCtl {
     float eps_step;        // FP32 rounding of one position update, added per step
     int age;               // steps since the last build
     int max_age;           // rebuild at least this often (bounds FP32 offset drift)
-    int force;             // rebuild at the next step: 1 state changed, 2 state changed but the
-                           // list bins hold its exact bins (no FP64 re-binning needed)
+    int force;             // rebuild at the next step (the state changed)
     int rebuild;           // this step's decision (read by the gated kernels)
-    int exact_every;       // every exact_every-th build re-bins from the FP64 positions
-    int exact_now;         // this build does (the others move frames in FP32)
     int builds;            // builds decided so far
     unsigned long long body_runs;  // builds actually run (counted by the first build kernel)
     unsigned long long overflow;   // slots whose list exceeded the capacity (last build)
@@ -45,7 +42,8 @@ struct ListCtl {
 
 constexpr int kNbrCap = 32;          // list entries per slot (more: the slot walks its stencil)
 constexpr int kNbrInline = 3;        // entries held in the slot's list record beside its metadata
-constexpr int kNbrShift = 26;        // entry = slot | (bin shifts << 26)
+constexpr int kNbrShift = 31;        // entries are slots below 2^31
+constexpr int kPairCap = 32;         // gated pairs per slot the step records when asked
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
 constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
 constexpr int kListBuildBlock = 128; // k_list_build's block (one slot per thread)
@@ -95,11 +93,18 @@ struct DevState {
     double *fc;        // 6 planes, force gather of the rod path
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
-    int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry:
-                       // neighbour slot | bin shifts dx, dy, dz in -1..1 as signed 2-bit
-                       // fields at bits 26-27, 28-29, 30-31
-    int4 *lrec;        // per slot: x = z bin (bits 0-15), edge flags (16-18), list length
-                       // (20-27, saturating); y, z, w = the first kNbrInline entries
+    int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry: the
+                       // neighbour slot (periodic images need no code: the fixed-point
+                       // difference is the minimum image)
+    int4 *lrec;        // per slot: x = list length (saturating at 255); y, z, w = the
+                       // first kNbrInline entries
+    int4 *fxh[2];      // list path positions, ping-pong with x/y/z: high 32 bits of the
+                       // 64-bit fixed-point x, y, z (FxGeom) and the FP32 radius bits --
+                       // what a neighbour gathers
+    unsigned *fxl[2];  // the low 32 bits, three planes of n (x, y, z)
+    const FxGeom *fxg; // per colony
+    int *pcap;         // null, or per slot 1 + kPairCap ints: the gated pairs of the last
+                       // list step (count, then neighbour slots in accumulation order)
     int *cellcnt;      // per 3D cell counter, zero between uses
     int *cellstart;    // ncells_total + 1 offsets of the cells in the sorted copies
     int ncells_total;
@@ -164,6 +169,10 @@ int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, 
 // decide: fold the last step's displacement into the bound and decide
 // whether this step rebuilds; sets the graph conditional `cond` when use_cond
 int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond, cudaStream_t st);
+// fixed-point positions of buffer a from its FP64 positions and radii (when the
+// list starts on a state), and back (whenever the FP64 positions are read)
+int launch_list_init(const DevState &S, int a, int grid, int block, cudaStream_t st);
+int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStream_t st);
 // rebuild (gated on lctl->rebuild): bins of buffer a's positions into the
 // list bins, column lists, and the list itself
 // (returns the kernels it enqueues, kListBodyKernels)

@@ -2,8 +2,8 @@
 //
 // The force acts only on pairs closer than rA = r_i + r_j + bw
 // (maxInteractionDistance and the gate r^2 <= (r_lm - 1e-15)^2,
-// bmx_cell_interaction_K.H:23-40, bmx_pc_interaction.cpp:212).  When
-// rA + skin is at most the smallest bin width, any pair that close sits in
+// bmx_cell_interaction_K.H:23-40, bmx_pc_interaction.cpp:212).  When the
+// largest rA is at most the smallest bin width, any pair that close sits in
 // neighbouring bins, so the reference's stencil list holds it whatever the
 // binning is.  The list built here holds every pair closer than rA + skin
 // at build time; while no pair's separation has changed by the skin since,
@@ -11,23 +11,34 @@
 // therefore the reference's; only the FP32 rounding of the pair math (the
 // precision form) differs from it.
 //
-// Between builds the bins stay frozen (buffer kListBins) and the FP32
-// offsets advance in the frozen frame, while the FP64 positions accumulate
-// and wrap periodically every step as in the reference.  A build moves
-// every frame to the bin its offset has reached (every kListExactEvery-th
-// build re-bins exactly from the FP64 positions instead, which also bounds
-// the FP32 drift of the offsets), rebuilds the cell lists and walks the
-// stencil once.  The bins need not be the reference's here: with
-// rA + skin within a bin width, any binning finds the same pairs.
+// State: while the list path runs, positions live in 64-bit fixed point
+// (FxGeom: one unit is span / 2^64, 7e-21 cm on a 0.128 cm box, finer than
+// the FP64 ulp anywhere above 2^-9 cm) as a 16-byte record per slot (the high
+// 32 bits of x, y, z and the FP32 radius) and three 32-bit low words.  A
+// step reads and writes those 28 bytes, reads the list and writes the FP32
+// velocity; a neighbour's offset is the int32 difference of two high words
+// (exact; the minimum periodic image by the unsigned wrap), converted once to
+// FP32 -- one 16-byte gather per neighbour, the same line its owner reads.
+// The FP32 increment, scaled to units to 2^-44 of itself, is added exactly:
+// no rounding accumulates in the positions, and no FP64 instruction runs
+// (GB300 issues FP64 at 1/64 of the FP32 rate).  The FP64 positions are converted from the
+// fixed point whenever anything reads them (launch_list_to_fp64), and to it
+// when the list path starts.
 // k_list_decide bounds the separation change of every pair from the spread
 // of each step's increments and asks for a build when the bound reaches the
 // skin (or after max_age steps); inside a CUDA graph the build kernels sit
 // in a conditional node that the decision switches, so a step without a
 // build launches two kernels.
 //
-// Roofline: the step kernel streams the slot state (FP64 positions in and
-// out, FP32 offsets in and out, FP32 velocities out) and the list; the
-// neighbour offsets it gathers are L2-resident.  HBM bound, no contraction.
+// Build: bins from the high words (integer arithmetic, consistent with the
+// positions), a counting sort into 3D cells, the in-cell order by caller
+// index (deterministic lists and FP32 summation order), and the stencil walk
+// that keeps every candidate within rA + skin on exact fixed-point
+// differences.
+//
+// Roofline: the step kernel streams 28 bytes of position state in and out,
+// the list in and the FP32 velocity out; the neighbour records it gathers
+// are L2-resident.  HBM bound, no contraction.
 #include <algorithm>
 
 #include "bmxg_stencil.cuh"
@@ -35,8 +46,6 @@
 namespace bmxg {
 
 namespace {
-
-constexpr unsigned kSlotMask = (1u << kNbrShift) - 1u;
 
 // Order-preserving unsigned key of a float (and back): atomicMin / atomicMax
 // on the keys order the floats.
@@ -54,13 +63,37 @@ __device__ __forceinline__ float funkey(unsigned k)
 constexpr unsigned kKeyPosInf = 0xff800000u;  // fkey(+inf)
 constexpr unsigned kKeyNegInf = 0x007fffffu;  // fkey(-inf)
 
+// An FP32 increment f in fixed-point units, f 2^64 / span, with the constant
+// as an FP32 pair c + cl (2^-48 of it): p = f c rounded, its exact error from
+// an FMA, plus f cl; each part rounded to the nearest unit.  Within 2^-44 of
+// the increment (and a few units: ~1e-19 cm on a 0.128 cm box), far below
+// the FP64 position's own rounding; the sum into the position is exact, so
+// no rounding accumulates however small the increment is against the
+// position.  An increment of a quarter span or more (or a non-finite one)
+// sets `big`.
+__device__ __forceinline__ long long fx_inc(float f, float c, float cl, bool &big)
+{
+    const float p = __fmul_rn(f, c);
+    if (!(fabsf(p) < 4.6116860184273879e18f)) {  // 2^62
+        big = true;
+        return 0ll;
+    }
+    const float r = __fmaf_rn(f, cl, __fmaf_rn(f, c, -p));
+    return __float2ll_rn(p) + __float2ll_rn(r);
+}
+
+__device__ __forceinline__ unsigned long long fx_join(unsigned h, unsigned l)
+{
+    return ((unsigned long long)h << 32) | l;
+}
+
 // The bound: for any pair, the separation change since the build is, per
 // component, at most the sum over steps of the spread (largest minus
 // smallest) of that step's increments; its length at most the length of
 // those sums.  Unlike twice the largest displacement, it does not count a
 // drift common to all slots (here: the rise of the slots below the growth
 // surface).  Each step adds eps_step per component for the FP32 rounding of
-// the offset updates.
+// the pair offsets the gate sees.
 // It also clears the per-step counters (no memset nodes in the step).
 __global__ void k_list_decide(ListCtl *c, DevCounters *cnt, cudaGraphConditionalHandle h, int use_h)
 {
@@ -84,9 +117,6 @@ __global__ void k_list_decide(ListCtl *c, DevCounters *cnt, cudaGraphConditional
     const int age = c->age + 1;
     const bool rb = c->force != 0 || !(acc <= c->skin) || age > c->max_age;
     if (rb) {
-        // force 1: state changed, bins unknown (exact); force 2: the list bins
-        // are already the exact bins of the positions (no FP64 re-binning)
-        c->exact_now = (c->force == 1 || (c->force == 0 && c->builds % c->exact_every == 0)) ? 1 : 0;
         for (int k = 0; k < 3; ++k) c->range[k] = 0.0f;
         c->acc = 0.0f;
         c->age = 0;
@@ -102,59 +132,39 @@ __global__ void k_list_decide(ListCtl *c, DevCounters *cnt, cudaGraphConditional
     if (use_h) cudaGraphSetConditional(h, rb ? 1u : 0u);
 }
 
-// Move one axis of a frozen frame to the bin the offset now falls in: the
-// offset leaves [0, w) by less than the skin between builds, so the bin moves
-// by at most one.  Periodic axes wrap the bin index (bin n + 1 is bin 1 one
-// period on, the frame the FP64 wrap of the position matches); on a closed
-// axis a bin outside 1..n keeps its frame, as bin_of clamps there.
-__device__ __forceinline__ void reframe(float &r, int &b, float w, int nb, int per)
-{
-    const int s = (r < 0.0f) ? -1 : ((r >= w) ? 1 : 0);
-    int nbin = b + s;
-    if (per) {
-        nbin = (nbin < 1) ? nbin + nb : ((nbin > nb) ? nbin - nb : nbin);
-    } else if (nbin < 1 || nbin > nb) {
-        return;
-    }
-    r -= (float)s * w;
-    b = nbin;
-}
-
 __device__ __forceinline__ int cell_of(const DevGeom &G, int bx, int by, int bz)
 {
     return G.cell_base + ((bx - 1) * G.n[1] + (by - 1)) * G.n[2] + (bz - 1);
 }
 
-// Bins of the list frames: every exact_every-th build (and the first) bins
-// buffer a's FP64 positions exactly and re-derives the FP32 offsets from
-// them (rebin_slot_into); the others move each frame by the bin its FP32
-// offset has reached, without FP64 arithmetic (GB300 issues FP64 at 1/64 of
-// the FP32 rate).  Either way the 3D cell counts are accumulated.
+// Bin of a high word: a periodic axis spans the domain (bin = h n / 2^32);
+// a closed axis has the domain in [2^30, 2^31), clamped to 1..n.
+__device__ __forceinline__ int fx_bin(unsigned h, int nb, int per)
+{
+    if (per) return (int)__umulhi(h, (unsigned)nb) + 1;
+    const long long d = (long long)h - (1ll << 30);
+    if (d < 0) return 1;
+    const long long b = (d * nb) >> 30;
+    return (b >= nb) ? nb : (int)b + 1;
+}
+
+// Bins of buffer a's fixed-point positions into the list bins (kListBins
+// buffer) and the 3D cell counts.
 __global__ void k_list_rebin(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
-    const bool exact = S.lctl->exact_now != 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) S.lctl->body_runs += 1ull;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-        const DevGeom &G = geom_of(S, i);
-        int bx, by, bz;
-        if (exact) {
-            // (the column counters are the per-step paths'; the list counts cells)
-            rebin_slot_into(S, G, i, S.x[a][i], S.y[a][i], S.z[a][i], S.rad[i], B, a, false, false);
-            col_to_bxy(G, S.col[B][i], bx, by);
-            bz = S.iz[B][i];
-        } else {
-            float4 r = S.rel[a][i];
-            col_to_bxy(G, S.col[B][i], bx, by);
-            bz = S.iz[B][i];
-            reframe(r.x, bx, G.dxf[0], G.n[0], G.per[0]);
-            reframe(r.y, by, G.dxf[1], G.n[1], G.per[1]);
-            reframe(r.z, bz, G.dxf[2], G.n[2], 0);
-            S.col[B][i] = column_of(G, bx, by);
-            S.iz[B][i] = bz;
-            S.rel[a][i] = r;
-        }
+        const int col = colony_of(S.cbase, S.ncol, i);
+        const DevGeom &G = S.geoms[col];
+        const FxGeom &F = S.fxg[col];
+        const int4 h = S.fxh[a][i];
+        const int bx = fx_bin((unsigned)h.x, F.n[0], F.per[0]);
+        const int by = fx_bin((unsigned)h.y, F.n[1], F.per[1]);
+        const int bz = fx_bin((unsigned)h.z, F.n[2], F.per[2]);
+        S.col[B][i] = column_of(G, bx, by);
+        S.iz[B][i] = bz;
         atomicAdd(&S.cellcnt[cell_of(G, bx, by, bz)], 1);
     }
 }
@@ -177,7 +187,8 @@ __global__ void k_list_scatter(const DevState S)
 }
 
 // deterministic order inside a cell (ascending original index), and the
-// sorted copies the build walks: offsets, z bin, slot, and each slot's rank
+// sorted copies the build walks: the position record, z bin, slot, and each
+// slot's rank
 __global__ void k_list_canon(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
@@ -201,7 +212,7 @@ __global__ void k_list_canon(const DevState S, int a)
             continue;
         }
         S.perm[B][t] = i;
-        S.srel[B][t] = S.rel[a][i];
+        reinterpret_cast<int4 *>(S.srel[B])[t] = S.fxh[a][i];
         S.siz[B][t] = bz;
         S.rank[B][i] = t;
     }
@@ -209,11 +220,9 @@ __global__ void k_list_canon(const DevState S, int a)
 
 // Visit the slots of the 3 x 3 neighbour columns of bin (bx, by), z bins
 // izi - 1 .. izi + 1 (periodic images included), as contiguous cell ranges
-// of the sorted copies.  f(u, dxs, dys, dzs): sorted position and the bin
-// shift of the neighbour relative to (bx, by, izi); the slot's own sorted
-// position self_t is skipped.  (One loop per column over its three z cells
-// keeps the lanes of a warp together better than a loop per cell; a
-// candidate's z bin follows from the cell boundaries inside the range.)
+// of the sorted copies: f(u) for each sorted position u but the slot's own
+// self_t.  Order: x rows outermost, then y, then z, ascending caller index
+// within a cell.
 template <class F>
 __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G, int self_t, int bx, int by, int izi,
                                             F &&f)
@@ -235,75 +244,86 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
             }
             const int cb = G.cell_base + ((sx - 1) * G.n[1] + (sy - 1)) * nz;
             const int hi = __ldg(&cs[cb + z1]);
-            // z bin of a candidate from the cell boundaries inside the range
-            const int m1 = __ldg(&cs[cb + z0]), m2 = (z1 > z0) ? __ldg(&cs[cb + z0 + 1]) : hi;
-            const int dz0 = z0 - izi;
             for (int u = __ldg(&cs[cb + z0 - 1]); u < hi; ++u) {
                 if (u == self_t) continue;
-                f(u, dxs, dys, dz0 + (u >= m1) + (u >= m2));
+                f(u);
             }
         }
     }
 }
 
 // List build: every slot (in sorted order, so a warp's lanes share cells)
-// keeps the neighbours closer than rA + skin (+ a slack covering the FP32
-// rounding of the test), and its packed metadata: z bin, edge flags (x or y
-// bin on a periodic face, z bin at a closed face) and list length.
+// keeps the neighbours closer than rA + skin on the exact fixed-point
+// differences of the high words (+ a slack of four units per component and
+// the FP32 rounding of the test), and its list length.
 __global__ void __launch_bounds__(kListBuildBlock) k_list_build(const DevState S, const DevParams P)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
     const int n = S.n;
     const float reach = P.bw32 + S.lctl->skin;
+    const int4 *__restrict__ sg = reinterpret_cast<const int4 *>(S.srel[B]);
     unsigned long long over = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int i = S.perm[B][t];
-        const DevGeom &G = geom_of(S, i);
+        const int col = colony_of(S.cbase, S.ncol, i);
+        const DevGeom &G = S.geoms[col];
+        const FxGeom &F = S.fxg[col];
         int bx, by;
         col_to_bxy(G, S.col[B][i], bx, by);
         const int izi = S.siz[B][t];
-        const float4 me = S.srel[B][t];
-        const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
-        const float lim0 = reach + 4.0e-6f * fmaxf(dxb, fmaxf(dyb, dzb));
+        const int4 me = sg[t];
+        const float ux = F.uh[0], uy = F.uh[1], uz = F.uh[2];
+        const float ri = __int_as_float(me.w);
+        const float lim0 = reach + 4.0f * (ux + uy + uz);
         int c = 0;
         int4 rec = make_int4(0, 0, 0, 0);
-        visit_cells(S, G, t, bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
-            const float4 q = __ldg(&S.srel[B][u]);
-            const float ex = (me.x - q.x) - (float)dxs * dxb;
-            const float ey = (me.y - q.y) - (float)dys * dyb;
-            const float ez = (me.z - q.z) - (dzs == 0 ? 0.0f : (dzs > 0 ? dzb : -dzb));
+        visit_cells(S, G, t, bx, by, izi, [&](int s) {
+            const int4 q = __ldg(&sg[s]);
+            const float ex = (float)(me.x - q.x) * ux;
+            const float ey = (float)(me.y - q.y) * uy;
+            const float ez = (float)(me.z - q.z) * uz;
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float lim = (me.w + q.w) + lim0;
+            const float lim = ((ri + __int_as_float(q.w)) + lim0) * 1.000001f;
             if (!(r2f <= lim * lim)) return;
-            const unsigned code = (unsigned)(dxs & 3) | ((unsigned)(dys & 3) << 2) | ((unsigned)(dzs & 3) << 4);
-            const int e = (int)((unsigned)__ldg(&S.perm[B][u]) | (code << kNbrShift));
+            const int e = __ldg(&S.perm[B][s]);
             if (c == 0) rec.y = e;
             else if (c == 1) rec.z = e;
             else if (c == 2) rec.w = e;
             else if (c < kNbrCap) S.nbr[(size_t)(c - kNbrInline) * n + i] = e;
             ++c;
         });
-        const int edge = ((G.per[0] && (bx == 1 || bx == G.n[0])) ? 1 : 0) |
-                         ((G.per[1] && (by == 1 || by == G.n[1])) ? 2 : 0) | ((izi == 1 || izi == G.n[2]) ? 4 : 0);
-        rec.x = izi | (edge << 16) | (min(c, 255) << 20);
+        rec.x = min(c, 255);
         S.lrec[i] = rec;
         if (c > kNbrCap) ++over;
     }
     if (over) atomicAdd(&S.lctl->overflow, over);
 }
 
-// FP32F sphere step over the list: pair math and wall law in FP32 on the
-// frozen-frame offsets, FP64 position accumulation; the periodic wrap and
-// the domain test (FP64 compares) only run for slots whose frozen bin is on
-// a face, the only ones that can cross it before the next build.
+// Gated pairs of a step, recorded when the context asks (S.pcap): per slot,
+// the count and the neighbour slots the step accumulated, in its order.
+struct PairRec {
+    int *cap;
+    int i, k;
+    __device__ __forceinline__ void add(int j)
+    {
+        if (cap && k < kPairCap) cap[(size_t)i * (kPairCap + 1) + 1 + k] = j;
+        ++k;
+    }
+    __device__ __forceinline__ void done()
+    {
+        if (cap) cap[(size_t)i * (kPairCap + 1)] = k;
+    }
+};
+
+// FP32F sphere step over the list: pair offsets from the fixed-point high
+// words, pair math and wall law in FP32, the increments added in 64-bit fixed
+// point (the periodic wrap is the unsigned wrap; the domain test of the
+// closed z axis compares the high word).
 // Each block takes a contiguous chunk of slots, so a thread's colony is
 // found by one binary search and then by stepping forward from the last one.
 // The list metadata and the first entries come in one 16-byte record.
-// (128, 12): 40 registers without spills, twelve blocks of four warps per SM;
-// the kernel is latency bound and wants every resident warp (128-thread
-// blocks: 92.4 us against 94.3 us with 256 threads in six blocks, the block
-// scheduler balancing the uneven lists at a finer grain)
+template <bool CAP>
 __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
 {
     constexpr int B = kListBins;
@@ -311,7 +331,8 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
     const int n = S.n;
     const float bwf = P.bw32, kf = P.k32;
     const float zkf = P.z_k32, zbwf = P.z_bw32, zgf = P.z_g32;
-    const float4 *__restrict__ rel_a = S.rel[a];
+    const int4 *__restrict__ ga = S.fxh[a];
+    const unsigned *__restrict__ la = S.fxl[a];
     const int *__restrict__ nbr = S.nbr;
     // smallest and largest increment per component (order-preserving keys),
     // per warp in shared memory: reduced over the warp after each pass, so
@@ -332,105 +353,107 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
         unsigned hi0 = kKeyNegInf, hi1 = kKeyNegInf, hi2 = kKeyNegInf;
         if (i < i1) {
             while (colony + 1 < S.ncol && __ldg(&S.cbase[colony + 1]) <= i) ++colony;
-            const DevGeom &G = S.geoms[colony];
-            const float4 me = rel_a[i];
+            const FxGeom &F = S.fxg[colony];
             const int4 rec = __ldg(&S.lrec[i]);
-            const int meta = rec.x;
-            const int izi = meta & 0xffff;
-            const int edge = (meta >> 16) & 7;
-            const int cnt = meta >> 20;
-            const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
+            const int4 h = ga[i];
+            const int cnt = rec.x & 0xff;
+            const float4 fu = *reinterpret_cast<const float4 *>(F.uh);  // units and the growth surface
+            const float ux = fu.x, uy = fu.y, uz = fu.z;
+            const unsigned zw = __float_as_uint(fu.w);
+            const float ri = __int_as_float(h.w);
             float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-            auto pair = [&](const float4 q, float ox, float oy, float oz) {
-                const float ex = (me.x - q.x) - ox;
-                const float ey = (me.y - q.y) - oy;
-                const float ez = (me.z - q.z) - oz;
+            PairRec pr{CAP ? S.pcap : nullptr, i, 0};
+            auto pair = [&](int j, const int4 q) {
+                const float ex = (float)(h.x - q.x) * ux;
+                const float ey = (float)(h.y - q.y) * uy;
+                const float ez = (float)(h.z - q.z) * uz;
                 const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-                const float rSf = __fadd_rn(me.w, q.w);
+                const float rSf = __fadd_rn(ri, __int_as_float(q.w));
                 const float rAf = __fadd_rn(rSf, bwf);
                 if (!(r2f < __fmul_rn(rAf, rAf))) return;
+                if (CAP) pr.add(j);
                 const float inv = rsqrtf(r2f);
                 const float rn = __fmul_rn(r2f, inv);
                 const float d1 = __fsub_rn(rn, rAf);
-                const float F = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
-                const float Fi = __fmul_rn(F, inv);
+                const float Fm = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
+                const float Fi = __fmul_rn(Fm, inv);
                 gx = __fmaf_rn(Fi, ex, gx);
                 gy = __fmaf_rn(Fi, ey, gy);
                 gz = __fmaf_rn(Fi, ez, gz);
             };
             if (cnt <= kNbrCap) {
-                auto entry = [&](unsigned e, const float4 q) {
-                    // signed 2-bit shifts at bits 26-27, 28-29, 30-31
-                    pair(q, (float)((int)(e << 4) >> 30) * dxb, (float)((int)(e << 2) >> 30) * dyb,
-                         (float)((int)e >> 30) * dzb);
-                };
                 // the first entries came with the metadata: their gathers go out
                 // together, one round trip for the typical short list
-                const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                const float4 p0 = (cnt > 0) ? __ldg(&rel_a[(unsigned)rec.y & kSlotMask]) : z4;
-                const float4 p1 = (cnt > 1) ? __ldg(&rel_a[(unsigned)rec.z & kSlotMask]) : z4;
-                const float4 p2 = (cnt > 2) ? __ldg(&rel_a[(unsigned)rec.w & kSlotMask]) : z4;
-                if (cnt > 0) entry((unsigned)rec.y, p0);
-                if (cnt > 1) entry((unsigned)rec.z, p1);
-                if (cnt > 2) entry((unsigned)rec.w, p2);
+                const int4 z4 = make_int4(0, 0, 0, 0);
+                const int4 p0 = (cnt > 0) ? __ldg(&ga[rec.y]) : z4;
+                const int4 p1 = (cnt > 1) ? __ldg(&ga[rec.z]) : z4;
+                const int4 p2 = (cnt > 2) ? __ldg(&ga[rec.w]) : z4;
+                if (cnt > 0) pair(rec.y, p0);
+                if (cnt > 1) pair(rec.z, p1);
+                if (cnt > 2) pair(rec.w, p2);
                 const int *col = nbr + i;  // entry k in plane k - kNbrInline
                 int k = kNbrInline;
                 // four entries in flight at a time: the list loads and the
                 // neighbour gathers are independent across entries
                 for (; k + 4 <= cnt; k += 4) {
-                    const unsigned e0 = (unsigned)__ldg(col + (size_t)(k - kNbrInline) * n);
-                    const unsigned e1 = (unsigned)__ldg(col + (size_t)(k + 1 - kNbrInline) * n);
-                    const unsigned e2 = (unsigned)__ldg(col + (size_t)(k + 2 - kNbrInline) * n);
-                    const unsigned e3 = (unsigned)__ldg(col + (size_t)(k + 3 - kNbrInline) * n);
-                    const float4 q0 = __ldg(&rel_a[e0 & kSlotMask]);
-                    const float4 q1 = __ldg(&rel_a[e1 & kSlotMask]);
-                    const float4 q2 = __ldg(&rel_a[e2 & kSlotMask]);
-                    const float4 q3 = __ldg(&rel_a[e3 & kSlotMask]);
-                    entry(e0, q0);
-                    entry(e1, q1);
-                    entry(e2, q2);
-                    entry(e3, q3);
+                    const int e0 = __ldg(col + (size_t)(k - kNbrInline) * n);
+                    const int e1 = __ldg(col + (size_t)(k + 1 - kNbrInline) * n);
+                    const int e2 = __ldg(col + (size_t)(k + 2 - kNbrInline) * n);
+                    const int e3 = __ldg(col + (size_t)(k + 3 - kNbrInline) * n);
+                    const int4 q0 = __ldg(&ga[e0]);
+                    const int4 q1 = __ldg(&ga[e1]);
+                    const int4 q2 = __ldg(&ga[e2]);
+                    const int4 q3 = __ldg(&ga[e3]);
+                    pair(e0, q0);
+                    pair(e1, q1);
+                    pair(e2, q2);
+                    pair(e3, q3);
                 }
                 for (; k < cnt; ++k) {
-                    const unsigned e = (unsigned)__ldg(col + (size_t)(k - kNbrInline) * n);
-                    entry(e, __ldg(&rel_a[e & kSlotMask]));
+                    const int e = __ldg(col + (size_t)(k - kNbrInline) * n);
+                    pair(e, __ldg(&ga[e]));
                 }
-            } else {  // list overflow: walk the frozen cells with the current offsets
+            } else {  // list overflow: walk the build's cells with the current records
+                const DevGeom &G = S.geoms[colony];
                 int bx, by;
                 col_to_bxy(G, S.col[B][i], bx, by);
-                visit_cells(S, G, S.rank[B][i], bx, by, izi, [&](int u, int dxs, int dys, int dzs) {
-                    pair(__ldg(&S.rel[a][__ldg(&S.perm[B][u])]), (float)dxs * dxb, (float)dys * dyb,
-                         (float)dzs * dzb);
+                visit_cells(S, G, S.rank[B][i], bx, by, S.iz[B][i], [&](int s) {
+                    const int j = __ldg(&S.perm[B][s]);
+                    pair(j, __ldg(&ga[j]));
                 });
             }
-            float dzw;
-            if (izi < G.nwz) {
-                const float2 c = G.wz[izi];
-                dzw = (c.x + me.z) + c.y;
-            } else {
-                dzw = (float)(S.z[a][i] - P.z_wall);
-            }
-            const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, me.w, zkf, zbwf, zgf);
+            if (CAP) pr.done();
+            const float dzw = (float)(int)((unsigned)h.z - zw) * uz;
+            const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, ri, zkf, zbwf, zgf);
             const float ix = dtf * vx, iy = dtf * vy, iz = dtf * vz;
-            double nx = S.x[a][i] + f2d_int(ix);
-            double ny = S.y[a][i] + f2d_int(iy);
-            const double nz = S.z[a][i] + f2d_int(iz);
-            if (edge) {
-                if (edge & 1) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
-                if (edge & 2) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
-                if ((edge & 4) && !(nz >= G.plo[2] && nz < G.phi[2])) atomicAdd(&S.cnt->out_of_domain, 1ULL);
+            bool big = false;
+            const float4 fc = *reinterpret_cast<const float4 *>(F.c);
+            const float4 fl = *reinterpret_cast<const float4 *>(F.cl);
+            const unsigned long long nx =
+                fx_join((unsigned)h.x, la[i]) + (unsigned long long)fx_inc(ix, fc.x, fl.x, big);
+            const unsigned long long ny =
+                fx_join((unsigned)h.y, la[n + i]) + (unsigned long long)fx_inc(iy, fc.y, fl.y, big);
+            const unsigned long long nz =
+                fx_join((unsigned)h.z, la[2 * (size_t)n + i]) + (unsigned long long)fx_inc(iz, fc.z, fl.z, big);
+            const unsigned hz = (unsigned)(nz >> 32);
+            // the domain [plo, phi) of a closed axis is the high word in [2^30, 2^31)
+            if (hz - (1u << 30) >= (1u << 30)) {
+                atomicAdd(&S.cnt->out_of_domain, 1ULL);
+                // within three quarters of a length of the domain, or the fixed point's range ends
+                if (hz < (1u << 28) || hz >= 0xf0000000u) atomicAdd(&S.cnt->range, 1ULL);
             }
-            S.x[b][i] = nx;
-            S.y[b][i] = ny;
-            S.z[b][i] = nz;
-            S.rel[b][i] = make_float4(me.x + ix, me.y + iy, me.z + iz, me.w);
+            S.fxh[b][i] = make_int4((int)(nx >> 32), (int)(ny >> 32), (int)hz, h.w);
+            unsigned *lb = S.fxl[b];
+            lb[i] = (unsigned)nx;
+            lb[n + i] = (unsigned)ny;
+            lb[2 * (size_t)n + i] = (unsigned)nz;
             S.vxf[i] = vx;
             S.vyf[i] = vy;
             S.vzf[i] = vz;
             lo0 = hi0 = fkey(ix);
             lo1 = hi1 = fkey(iy);
             lo2 = hi2 = fkey(iz);
-            if (!isfinite(ix + iy + iz)) {
+            if (!isfinite(ix + iy + iz) || big) {
                 atomicAdd(&S.cnt->nonfinite, 1ULL);
                 lo0 = 0u;  // spreads the bound: the next step rebuilds
                 hi0 = 0xffffffffu;
@@ -468,11 +491,72 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
     }
 }
 
+// fixed point of a coordinate: (x - o) / u mod 2^64 on a periodic axis, else
+// clamped to the range (a closed axis's range is four domain lengths)
+__device__ __forceinline__ unsigned long long to_fx(double x, double o, double u, int per)
+{
+    double t = (x - o) / u;
+    const double two64 = 18446744073709551616.0;
+    if (per) t -= floor(t / two64) * two64;
+    if (!(t >= 0.0)) t = 0.0;
+    if (t >= two64) t = two64 - 4096.0;
+    return __double2ull_rn(t);
+}
+
+// Fixed-point positions of buffer a from its FP64 positions and the radii
+__global__ void k_list_init(const DevState S, int a)
+{
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const FxGeom &F = S.fxg[colony_of(S.cbase, S.ncol, i)];
+        const unsigned long long X = to_fx(S.x[a][i], F.o[0], F.u[0], F.per[0]);
+        const unsigned long long Y = to_fx(S.y[a][i], F.o[1], F.u[1], F.per[1]);
+        const unsigned long long Z = to_fx(S.z[a][i], F.o[2], F.u[2], F.per[2]);
+        S.fxh[a][i] = make_int4((int)(X >> 32), (int)(Y >> 32), (int)(Z >> 32), __float_as_int(d2f_rn(S.rad[i])));
+        S.fxl[a][i] = (unsigned)X;
+        S.fxl[a][n + i] = (unsigned)Y;
+        S.fxl[a][2 * (size_t)n + i] = (unsigned)Z;
+    }
+}
+
+// FP64 position of a fixed-point coordinate (a periodic one kept below phi)
+__device__ __forceinline__ double from_fx(unsigned long long X, double o, double u, int per, double phi)
+{
+    double x = o + __ull2double_rn(X) * u;
+    if (per && !(x < phi)) x = nextafter(phi, -1.0e300);
+    return x;
+}
+
+// FP64 positions of buffer a from its fixed-point positions
+__global__ void k_list_to_fp64(const DevState S, int a)
+{
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const FxGeom &F = S.fxg[colony_of(S.cbase, S.ncol, i)];
+        const int4 h = S.fxh[a][i];
+        S.x[a][i] = from_fx(fx_join((unsigned)h.x, S.fxl[a][i]), F.o[0], F.u[0], F.per[0], F.phi[0]);
+        S.y[a][i] = from_fx(fx_join((unsigned)h.y, S.fxl[a][n + i]), F.o[1], F.u[1], F.per[1], F.phi[1]);
+        S.z[a][i] = from_fx(fx_join((unsigned)h.z, S.fxl[a][2 * (size_t)n + i]), F.o[2], F.u[2], F.per[2], F.phi[2]);
+    }
+}
+
 }  // namespace
 
 int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond, cudaStream_t st)
 {
     k_list_decide<<<1, 1, 0, st>>>(S.lctl, S.cnt, (cudaGraphConditionalHandle)cond, use_cond);
+    return 1;
+}
+
+int launch_list_init(const DevState &S, int a, int grid, int block, cudaStream_t st)
+{
+    k_list_init<<<grid, block, 0, st>>>(S, a);
+    return 1;
+}
+
+int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStream_t st)
+{
+    k_list_to_fp64<<<grid, block, 0, st>>>(S, a);
     return 1;
 }
 
@@ -486,8 +570,7 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     k_list_canon<<<grid, block, 0, st>>>(S, a);
     // the build: one slot per thread in 128-thread blocks (the stencil walks
     // differ in length from slot to slot; small blocks on a grid of every
-    // slot let the scheduler balance them: 150.0 -> 145.7 us per whole step
-    // against 256-thread blocks striding over one wave)
+    // slot let the scheduler balance them)
     k_list_build<<<(S.n + kListBuildBlock - 1) / kListBuildBlock, kListBuildBlock, 0, st>>>(S, P);
     return k + 3;
 }
@@ -503,7 +586,9 @@ int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, in
     // (grid = the SM count): small states need the blocks more.
     const int two = (S.n + 2 * block - 1) / (2 * block);
     const int chunk = (two >= 4 * 12 * grid) ? 2 * block : block;
-    k_list_step<<<(S.n + chunk - 1) / chunk, block, 0, st>>>(S, P, (float)dt, a, chunk);
+    const int nb = (S.n + chunk - 1) / chunk;
+    if (S.pcap) k_list_step<true><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
+    else k_list_step<false><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
     return 1;
 }
 

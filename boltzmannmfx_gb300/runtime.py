@@ -27,7 +27,8 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
                "bmxg_particle_exchange", "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk",
                "bmxg_read_checkpoint",
-               "bmxg_io_last_error", "bmxg_autotune", "bmxg_split_cells_aos")
+               "bmxg_io_last_error", "bmxg_autotune", "bmxg_split_cells_aos", "bmxg_set_pair_capture",
+               "bmxg_get_step_pairs")
 
 
 class Ext(C.Structure):
@@ -73,6 +74,9 @@ def load_library(path=None):
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.bmxg_set_list_mode.argtypes = [vp, C.c_int32]
+    L.bmxg_set_pair_capture.argtypes = [vp, C.c_int32]
+    L.bmxg_get_step_pairs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int64,
+                                      C.POINTER(C.c_int64)]
     dp = C.POINTER(C.c_double)
     L.bmxg_particle_exchange.argtypes = [vp, dp, dp, C.c_double, dp, C.c_int32]
     PS = C.POINTER(ParticlesStruct)
@@ -203,6 +207,26 @@ class Context:
     def set_list_mode(self, mode):
         """1: FP32F sphere steps use the skin neighbour list where it is exact; 0: never."""
         self._check(self.lib.bmxg_set_list_mode(self.h, int(mode)))
+
+    def set_pair_capture(self, on):
+        """list steps record the pairs that pass the force gate (debug export)."""
+        self._check(self.lib.bmxg_set_pair_capture(self.h, 1 if on else 0))
+
+    def step_pairs(self):
+        """(offs, idx): the gated pairs the last FP32F list step accumulated, per
+        particle in original order, neighbours as original indices in the order
+        the step summed them (needs set_pair_capture(True) before the step)."""
+        offs = np.zeros(self.n + 1, np.int64)
+        total = C.c_int64(0)
+        rc = self.lib.bmxg_get_step_pairs(self.h, offs.ctypes.data_as(C.POINTER(C.c_int64)), None, 0,
+                                          C.byref(total))
+        if rc not in (abi.BMXG_OK, abi.BMXG_ERR_CAPACITY) or (rc == abi.BMXG_ERR_CAPACITY and total.value == 0):
+            self._check(rc)
+        idx = np.zeros(max(total.value, 1), np.int32)
+        self._check(self.lib.bmxg_get_step_pairs(self.h, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                 idx.ctypes.data_as(C.POINTER(C.c_int32)), total.value,
+                                                 C.byref(total)))
+        return offs, idx[:total.value]
 
     def init_bonds(self, rlim=1.0e-7):
         """InitBonds on the loaded state (bond tables of coincident segment

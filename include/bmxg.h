@@ -414,6 +414,21 @@ int  bmxg_read_checkpoint(const char *dir, int32_t level, bmxg_particles *out, i
 /* Message of the last failed fixture I/O call of this thread. */
 const char *bmxg_io_last_error(void);
 
+/* Gated pairs of the LAST FP32F list step, as that step accumulated them:
+ * with capture on (bmxg_set_pair_capture), every list step records, per
+ * particle, the neighbours whose pair passed the force gate r^2 < rA^2
+ * (bmx_pc_interaction.cpp:212) in the order the step summed them.  For
+ * particle i (original order) entries offs[i]..offs[i+1]-1 of idx hold the
+ * original indices of those neighbours (offs: n+1 entries; idx may be NULL
+ * for the counts only).  Returns BMXG_ERR_STATE when the last step was not a
+ * list step recorded with capture on, BMXG_ERR_CAPACITY (and *total) when
+ * cap is too small or a particle had more than 32 gated pairs.  A check of
+ * the list the step walks against the reference's gated pair set; it has no
+ * counterpart in the reference (AMReX's list holds every stencil pair and the
+ * gate runs inside the force loop). */
+int  bmxg_set_pair_capture(bmxg_ctx *ctx, int32_t on);
+int  bmxg_get_step_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int64_t cap, int64_t *total);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* FP32F sphere steps keep a neighbour list with a skin between builds when it

@@ -96,8 +96,9 @@ def test_graph_and_eager_steps_agree(gpu_lib):
     sa = A.stats()
     B.step(w.dt, 24, BMXG_FP32F)
     sb = B.stats()
-    # two kernels per step, seven per build
-    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 7 * sa["n_rebins"]
+    # two kernels per step, seven per build, and the list's set-up (the
+    # fixed-point positions) once
+    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 7 * sa["n_rebins"] + 1
     assert sa["n_rebins"] == sb["n_rebins"]
     QA, QB = read(A, w.particles), read(B, w.particles)
     for k in ("x", "y", "z", "velx", "vely", "velz"):
@@ -172,9 +173,45 @@ def test_list_batched_colonies(gpu_lib, oracle_lib):
     assert relerr(QA["z"] - P["z"], QB["z"] - P["z"]) <= 1e-4
 
 
-def test_position_accumulation_is_binary64(gpu_lib):
-    """The list step accumulates positions in FP64: the result equals
-    x + double(float(dt) * v) bit for bit (v the step's FP32 velocity)."""
+def test_list_position_accumulation(gpu_lib):
+    """The list path accumulates positions in 64-bit fixed point: after 24 list
+    steps a position equals its start plus the sum of the steps' FP32
+    increments float(dt) * v, summed in extended precision, within 4 FP64 ulp
+    plus 16 fixed-point units (the conversions in and out, and the ~1e-19 cm
+    of each increment's scaling to units); modulo the box in the periodic x
+    and y."""
+    w = configs.sphere_fp32(n=40_000)
+    g = w.geoms[0]
+    ctx = ctx_for(w)
+    ctx.step(w.dt, 2, BMXG_FP32F)   # builds the list (a first call of one step runs the per-step path)
+    P0 = read(ctx, w.particles)
+    acc = {k: P0[k].astype(np.longdouble) for k in ("x", "y", "z")}
+    dtf = np.float32(w.dt)
+    for s in range(24):
+        ctx.step(w.dt, 1, BMXG_FP32F)
+        Q = read(ctx, w.particles)
+        for k, v in (("x", "velx"), ("y", "vely"), ("z", "velz")):
+            acc[k] += (dtf * Q[v].astype(np.float32)).astype(np.longdouble)
+    assert ctx.stats()["n_rebins"] < 26
+    for d, k in enumerate(("x", "y", "z")):
+        want = acc[k]
+        if g.is_periodic[d]:
+            L = np.longdouble(g.prob_hi[d] - g.prob_lo[d])
+            want = want - L * np.floor((want - np.longdouble(g.prob_lo[d])) / L)
+        diff = np.abs(Q[k].astype(np.longdouble) - want)
+        if g.is_periodic[d]:
+            diff = np.minimum(diff, np.abs(diff - L))
+        ulp = np.spacing(np.abs(Q[k]))
+        # near 0 the FP64 ulp is finer than a fixed-point unit (span / 2^64)
+        span = (g.prob_hi[d] - g.prob_lo[d]) * (1.0 if g.is_periodic[d] else 4.0)
+        tol = 4 * ulp + 16 * np.ldexp(span, -64)
+        assert np.all(diff <= tol), (k, float((diff / tol).max()))
+
+
+def test_per_step_position_accumulation_is_binary64(gpu_lib):
+    """The per-step FP32F path (a one-step call right after a load) accumulates
+    positions in FP64: the result equals x + double(float(dt) * v) bit for bit
+    (v the step's FP32 velocity)."""
     w = configs.sphere_fp32(n=40_000)
     g = w.geoms[0]
     ctx = ctx_for(w)
