@@ -24,8 +24,11 @@ __global__ void k_bin(const DevState S, int b)
 }
 
 // ---- exclusive scan of n ints into n+1 offsets ----------------------------
+// Three passes: tile sums, a scan of the tile sums, the scan of each tile with
+// its offset.  A thread holds four consecutive counts, read and written as one
+// 16-byte vector (coalesced across the warp); a tile is 1024 counts.
 constexpr int kScanBlock = 256;
-constexpr int kScanItems = 16;
+constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanBlock * kScanItems;
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int &total)
@@ -56,16 +59,24 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int &total)
     return before + x - v;
 }
 
+// this thread's four counts (zero past n): one vector load where all four lie inside
+__device__ __forceinline__ int4 scan_load4(const int *__restrict__ in, int n, int base)
+{
+    if (base + 3 < n) return __ldg(reinterpret_cast<const int4 *>(in + base));
+    int4 v = make_int4(0, 0, 0, 0);
+    if (base < n) v.x = in[base];
+    if (base + 1 < n) v.y = in[base + 1];
+    if (base + 2 < n) v.z = in[base + 2];
+    return v;
+}
+
 __global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ bsum, const int *gate)
 {
     if (gate && !*gate) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    int s = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) s += in[base + k];
+    const int4 v = scan_load4(in, n, base);
     int total;
-    block_exclusive_scan(s, total);
+    block_exclusive_scan(v.x + v.y + v.z + v.w, total);
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
@@ -93,19 +104,16 @@ __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__res
 {
     if (gate && !*gate) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    int v[kScanItems];
-    int s = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = (base + k < n) ? in[base + k] : 0;
-        s += v[k];
-    }
+    const int4 v = scan_load4(in, n, base);
     int total;
-    int run = block_exclusive_scan(s, total) + bsum[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) out[base + k] = run;
-        run += v[k];
+    const int run = block_exclusive_scan(v.x + v.y + v.z + v.w, total) + bsum[blockIdx.x];
+    const int4 o = make_int4(run, run + v.x, run + v.x + v.y, run + v.x + v.y + v.z);
+    if (base + 3 < n) {
+        *reinterpret_cast<int4 *>(out + base) = o;
+    } else {
+        if (base < n) out[base] = o.x;
+        if (base + 1 < n) out[base + 1] = o.y;
+        if (base + 2 < n) out[base + 2] = o.z;
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = bsum[gridDim.x];
 }

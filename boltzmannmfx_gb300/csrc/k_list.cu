@@ -137,6 +137,22 @@ __device__ __forceinline__ int cell_of(const DevGeom &G, int bx, int by, int bz)
     return G.cell_base + ((bx - 1) * G.n[1] + (by - 1)) * G.n[2] + (bz - 1);
 }
 
+// Colony of index i for a kernel whose blocks take consecutive indices, one
+// per thread: one binary search per block (the colonies of a block's range
+// are few), then each thread steps forward.  Slot order and the list's sorted
+// order hold the colonies in the same ranges (a colony's particles stay
+// together under the sort), so either index works.  Every thread of the
+// block must call it (it synchronises the block).
+__device__ __forceinline__ int block_colony(const DevState &S, int i)
+{
+    __shared__ int c0;
+    if (threadIdx.x == 0) c0 = colony_of(S.cbase, S.ncol, min((int)(blockIdx.x * blockDim.x), S.n - 1));
+    __syncthreads();
+    int c = c0;
+    while (c + 1 < S.ncol && __ldg(&S.cbase[c + 1]) <= i) ++c;
+    return c;
+}
+
 // Bin of a high word: a periodic axis spans the domain (bin = h n / 2^32);
 // a closed axis has the domain in [2^30, 2^31), clamped to 1..n.
 __device__ __forceinline__ int fx_bin(unsigned h, int nb, int per)
@@ -155,8 +171,9 @@ __global__ void k_list_rebin(const DevState S, int a)
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
     if (blockIdx.x == 0 && threadIdx.x == 0) S.lctl->body_runs += 1ull;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-        const int col = colony_of(S.cbase, S.ncol, i);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < S.n) {
         const DevGeom &G = S.geoms[col];
         const FxGeom &F = S.fxg[col];
         const int4 h = S.fxh[a][i];
@@ -174,8 +191,10 @@ __global__ void k_list_scatter(const DevState S)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-        const DevGeom &G = geom_of(S, i);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < S.n) {
+        const DevGeom &G = S.geoms[col];
         int bx, by;
         col_to_bxy(G, S.col[B][i], bx, by);
         const int c = cell_of(G, bx, by, S.iz[B][i]);
@@ -193,8 +212,10 @@ __global__ void k_list_canon(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-        const DevGeom &G = geom_of(S, i);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < S.n) {
+        const DevGeom &G = S.geoms[col];
         int bx, by;
         col_to_bxy(G, S.col[B][i], bx, by);
         const int bz = S.iz[B][i];
@@ -209,12 +230,12 @@ __global__ void k_list_canon(const DevState S, int a)
         const int t = s0 + rank;
         if (t >= s1) {  // i is not among its cell's members: inconsistent counts
             atomicAdd(&S.cnt->bad_index, 1ULL);
-            continue;
+        } else {
+            S.perm[B][t] = i;
+            reinterpret_cast<int4 *>(S.srel[B])[t] = S.fxh[a][i];
+            S.siz[B][t] = bz;
+            S.rank[B][i] = t;
         }
-        S.perm[B][t] = i;
-        reinterpret_cast<int4 *>(S.srel[B])[t] = S.fxh[a][i];
-        S.siz[B][t] = bz;
-        S.rank[B][i] = t;
     }
 }
 
@@ -264,9 +285,10 @@ __global__ void __launch_bounds__(kListBuildBlock) k_list_build(const DevState S
     const float reach = P.bw32 + S.lctl->skin;
     const int4 *__restrict__ sg = reinterpret_cast<const int4 *>(S.srel[B]);
     unsigned long long over = 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, t);  // the sorted order keeps the colonies' ranges
+    if (t < n) {
         const int i = S.perm[B][t];
-        const int col = colony_of(S.cbase, S.ncol, i);
         const DevGeom &G = S.geoms[col];
         const FxGeom &F = S.fxg[col];
         int bx, by;
@@ -495,9 +517,9 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
 // clamped to the range (a closed axis's range is four domain lengths)
 __device__ __forceinline__ unsigned long long to_fx(double x, double o, double u, int per)
 {
-    double t = (x - o) / u;
     const double two64 = 18446744073709551616.0;
-    if (per) t -= floor(t / two64) * two64;
+    double t = (x - o) * (1.0 / u);  // a multiply by 2^64 / span (within FP64 rounding of the division)
+    if (per && !(t >= 0.0 && t < two64)) t -= floor(t * (1.0 / two64)) * two64;
     if (!(t >= 0.0)) t = 0.0;
     if (t >= two64) t = two64 - 4096.0;
     return __double2ull_rn(t);
@@ -507,8 +529,10 @@ __device__ __forceinline__ unsigned long long to_fx(double x, double o, double u
 __global__ void k_list_init(const DevState S, int a)
 {
     const int n = S.n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const FxGeom &F = S.fxg[colony_of(S.cbase, S.ncol, i)];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < n) {
+        const FxGeom &F = S.fxg[col];
         const unsigned long long X = to_fx(S.x[a][i], F.o[0], F.u[0], F.per[0]);
         const unsigned long long Y = to_fx(S.y[a][i], F.o[1], F.u[1], F.per[1]);
         const unsigned long long Z = to_fx(S.z[a][i], F.o[2], F.u[2], F.per[2]);
@@ -531,8 +555,10 @@ __device__ __forceinline__ double from_fx(unsigned long long X, double o, double
 __global__ void k_list_to_fp64(const DevState S, int a)
 {
     const int n = S.n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const FxGeom &F = S.fxg[colony_of(S.cbase, S.ncol, i)];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < n) {
+        const FxGeom &F = S.fxg[col];
         const int4 h = S.fxh[a][i];
         S.x[a][i] = from_fx(fx_join((unsigned)h.x, S.fxl[a][i]), F.o[0], F.u[0], F.per[0], F.phi[0]);
         S.y[a][i] = from_fx(fx_join((unsigned)h.y, S.fxl[a][n + i]), F.o[1], F.u[1], F.per[1], F.phi[1]);
@@ -550,13 +576,15 @@ int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond,
 
 int launch_list_init(const DevState &S, int a, int grid, int block, cudaStream_t st)
 {
-    k_list_init<<<grid, block, 0, st>>>(S, a);
+    (void)grid;  // one slot per thread
+    k_list_init<<<(S.n + block - 1) / block, block, 0, st>>>(S, a);
     return 1;
 }
 
 int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStream_t st)
 {
-    k_list_to_fp64<<<grid, block, 0, st>>>(S, a);
+    (void)grid;  // one slot per thread
+    k_list_to_fp64<<<(S.n + block - 1) / block, block, 0, st>>>(S, a);
     return 1;
 }
 
@@ -564,10 +592,12 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
                         cudaStream_t st)
 {
     const int *gate = &S.lctl->rebuild;
-    k_list_rebin<<<grid, block, 0, st>>>(S, a);
+    // one slot per thread (a block's colonies from one search)
+    const int g1 = (S.n + block - 1) / block;
+    k_list_rebin<<<g1, block, 0, st>>>(S, a);
     int k = 1 + launch_scan(S.cellcnt, S.cellstart, S.ncells_total, scan_scratch, st, gate);
-    k_list_scatter<<<grid, block, 0, st>>>(S);
-    k_list_canon<<<grid, block, 0, st>>>(S, a);
+    k_list_scatter<<<g1, block, 0, st>>>(S);
+    k_list_canon<<<g1, block, 0, st>>>(S, a);
     // the build: one slot per thread in 128-thread blocks (the stencil walks
     // differ in length from slot to slot; small blocks on a grid of every
     // slot let the scheduler balance them)
