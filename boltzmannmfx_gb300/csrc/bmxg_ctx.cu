@@ -357,6 +357,18 @@ void build_geoms(bmxg_ctx *ctx)
             F.per[d] = G.per[d];
             F.plo[d] = G.plo[d];
             F.phi[d] = G.phi[d];
+            F.ozero[d] = F.o[d] == 0.0 ? 1 : 0;
+            int k = 0;
+            const double fr = std::frexp(span, &k);  // span = fr 2^k, fr in [0.5, 1)
+            F.ms[d] = (unsigned long long)std::ldexp(fr, 53);
+            F.es[d] = k - 53;
+            // 2^64 / span = 2^(64 - es) / ms: q = 2^127 / ms, normalised to 64 bits
+            const unsigned __int128 q = ((unsigned __int128)1 << 127) / F.ms[d];
+            int bl = 0;
+            for (unsigned __int128 v = q; v; v >>= 1) ++bl;
+            const int sh = bl - 64;
+            F.mc[d] = (unsigned long long)(q >> sh);
+            F.ec[d] = (64 - F.es[d]) - 127 + sh;
         }
         {
             const long double t = ((long double)ctx->prm.z_wall - (long double)F.o[2]) / (long double)F.u[2];

@@ -75,6 +75,12 @@ struct alignas(16) FxGeom {
     int pad[2];
     double o[3], u[3];          // origin and unit (FP64: conversions at the path's ends)
     double plo[3], phi[3];      // the domain (clamp of converted periodic positions)
+    // integer conversions: span = ms 2^es exactly (ms the 53-bit significand),
+    // 2^64 / span = mc 2^ec with mc in [2^63, 2^64) (truncated)
+    unsigned long long ms[3], mc[3];
+    int es[3], ec[3];
+    int ozero[3];               // the origin is 0 (no FP64 addition)
+    int pad2;
 };
 
 // Counters a step accumulates on the device.

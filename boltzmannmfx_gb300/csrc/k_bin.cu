@@ -80,23 +80,46 @@ __global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-// one block over the nb tile sums: each thread scans a contiguous segment
-// serially, one block-wide scan joins the segments
-__global__ void k_scan_top(int *bsum, int nb, const int *gate)
+// one block of 1024 threads over the nb tile sums: each thread sums a
+// contiguous segment (its loads independent of each other), one block-wide
+// scan joins the segments, each thread writes its segment's offsets
+constexpr int kTopBlock = 1024;
+
+__global__ void __launch_bounds__(kTopBlock) k_scan_top(int *bsum, int nb, const int *gate)
 {
     if (gate && !*gate) return;
-    const int seg = (nb + kScanBlock - 1) / kScanBlock;
+    __shared__ int warp_sums[kTopBlock / 32];
+    const int seg = (nb + kTopBlock - 1) / kTopBlock;
     const int b0 = min((int)threadIdx.x * seg, nb), b1 = min(b0 + seg, nb);
     int s = 0;
+#pragma unroll 8
     for (int k = b0; k < b1; ++k) s += bsum[k];
-    int total;
-    int run = block_exclusive_scan(s, total);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    int run = ((warp > 0) ? warp_sums[warp - 1] : 0) + x - s;
     for (int k = b0; k < b1; ++k) {
         const int v = bsum[k];
         bsum[k] = run;
         run += v;
     }
-    if (threadIdx.x == 0) bsum[nb] = total;
+    if (threadIdx.x == 0) bsum[nb] = warp_sums[kTopBlock / 32 - 1];
 }
 
 __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__restrict__ bsum,
@@ -406,7 +429,7 @@ int launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t st, c
         return 0;
     }
     k_scan_reduce<<<nb, kScanBlock, 0, st>>>(in, n, scratch, gate);
-    k_scan_top<<<1, kScanBlock, 0, st>>>(scratch, nb, gate);
+    k_scan_top<<<1, kTopBlock, 0, st>>>(scratch, nb, gate);
     k_scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, scratch, out, gate);
     return 3;
 }

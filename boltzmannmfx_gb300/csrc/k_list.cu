@@ -513,16 +513,89 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
     }
 }
 
-// fixed point of a coordinate: (x - o) / u mod 2^64 on a periodic axis, else
-// clamped to the range (a closed axis's range is four domain lengths)
-__device__ __forceinline__ unsigned long long to_fx(double x, double o, double u, int per)
+// The two ends of the list path, in integer arithmetic (GB300 issues FP64 at
+// a small fraction of the FP32 rate; only an origin other than 0 costs one
+// FP64 addition or subtraction per coordinate).
+//
+// fixed point of a coordinate: (x - o) 2^64 / span, rounded, mod 2^64 on a
+// periodic axis, else clamped to the range [0, 2^64) (a closed axis's range
+// is four domain lengths from one length below plo).  With d = x - o =
+// md 2^ed and 2^64 / span = mc 2^ec the value is md mc 2^(ed + ec): a 117-bit
+// product shifted into place.
+__device__ __forceinline__ unsigned long long to_fx(double x, const FxGeom &F, int ax)
 {
-    const double two64 = 18446744073709551616.0;
-    double t = (x - o) * (1.0 / u);  // a multiply by 2^64 / span (within FP64 rounding of the division)
-    if (per && !(t >= 0.0 && t < two64)) t -= floor(t * (1.0 / two64)) * two64;
-    if (!(t >= 0.0)) t = 0.0;
-    if (t >= two64) t = two64 - 4096.0;
-    return __double2ull_rn(t);
+    const double d = F.ozero[ax] ? x : x - F.o[ax];
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int be = (int)((b >> 52) & 0x7ffu);
+    if (be == 0) return 0ull;  // zero (and subnormals)
+    const bool neg = (b >> 63) != 0ull;
+    const unsigned long long md = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+    const unsigned long long hi = __umul64hi(md, F.mc[ax]), lo = md * F.mc[ax];
+    const int r = -((be - 1075) + F.ec[ax]);  // X = (hi:lo) >> r
+    unsigned long long X;
+    bool over = false;
+    if (r <= 0) {
+        over = true;
+        X = 0ull;
+    } else if (r < 64) {
+        over = (hi >> r) != 0ull;
+        X = (hi << (64 - r)) | (lo >> r);
+        X += (lo >> (r - 1)) & 1ull;  // round half up
+    } else if (r < 128) {
+        X = (r == 64) ? hi : (hi >> (r - 64));
+        X += (r == 64) ? (lo >> 63) : ((hi >> (r - 65)) & 1ull);
+    } else {
+        X = 0ull;
+    }
+    if (F.per[ax]) return neg ? 0ull - X : X;  // the unsigned wrap is the periodic wrap
+    if (neg) return 0ull;
+    return over ? ~0ull : X;
+}
+
+// x of a fixed-point coordinate: o + X span / 2^64, the product X ms 2^(es - 64)
+// rounded to nearest even once (then the FP64 addition of a non-zero origin);
+// a periodic coordinate is kept below phi.
+__device__ __forceinline__ double from_fx(unsigned long long X, const FxGeom &F, int ax)
+{
+    const unsigned long long ms = F.ms[ax];
+    const unsigned long long hi = __umul64hi(X, ms), lo = X * ms;
+    unsigned long long t, rest;
+    int E;  // value = t 2^E with t in [2^63, 2^64), rest the bits below t
+    if (hi) {
+        const int lz = __clzll((long long)hi);
+        t = lz ? ((hi << lz) | (lo >> (64 - lz))) : hi;
+        rest = lo << lz;
+        E = F.es[ax] - lz;
+    } else if (lo) {
+        const int lz = __clzll((long long)lo);
+        t = lo << lz;
+        rest = 0ull;
+        E = F.es[ax] - 64 - lz;
+    } else {
+        t = 0ull;
+        rest = 0ull;
+        E = 0;
+    }
+    double v = 0.0;
+    if (t) {
+        unsigned long long m = t >> 11;
+        const unsigned long long rb = (t >> 10) & 1ull;
+        const bool sticky = (t & 0x3ffull) != 0ull || rest != 0ull;
+        m += rb & ((sticky ? 1ull : 0ull) | (m & 1ull));
+        if (m >> 53) {
+            m >>= 1;
+            ++E;
+        }
+        v = __longlong_as_double((long long)((((unsigned long long)(E + 1086)) << 52) | (m & 0xfffffffffffffull)));
+    }
+    if (F.ozero[ax]) {
+        // (periodic with plo = 0: v < len unless rounding reached it)
+        if (F.per[ax] && !(v < F.phi[ax])) v = nextafter(F.phi[ax], 0.0);
+        return v;
+    }
+    double x = F.o[ax] + v;
+    if (F.per[ax] && !(x < F.phi[ax])) x = nextafter(F.phi[ax], -1.0e300);
+    return x;
 }
 
 // Fixed-point positions of buffer a from its FP64 positions and the radii
@@ -533,22 +606,14 @@ __global__ void k_list_init(const DevState S, int a)
     const int col = block_colony(S, i);
     if (i < n) {
         const FxGeom &F = S.fxg[col];
-        const unsigned long long X = to_fx(S.x[a][i], F.o[0], F.u[0], F.per[0]);
-        const unsigned long long Y = to_fx(S.y[a][i], F.o[1], F.u[1], F.per[1]);
-        const unsigned long long Z = to_fx(S.z[a][i], F.o[2], F.u[2], F.per[2]);
+        const unsigned long long X = to_fx(S.x[a][i], F, 0);
+        const unsigned long long Y = to_fx(S.y[a][i], F, 1);
+        const unsigned long long Z = to_fx(S.z[a][i], F, 2);
         S.fxh[a][i] = make_int4((int)(X >> 32), (int)(Y >> 32), (int)(Z >> 32), __float_as_int(d2f_rn(S.rad[i])));
         S.fxl[a][i] = (unsigned)X;
         S.fxl[a][n + i] = (unsigned)Y;
         S.fxl[a][2 * (size_t)n + i] = (unsigned)Z;
     }
-}
-
-// FP64 position of a fixed-point coordinate (a periodic one kept below phi)
-__device__ __forceinline__ double from_fx(unsigned long long X, double o, double u, int per, double phi)
-{
-    double x = o + __ull2double_rn(X) * u;
-    if (per && !(x < phi)) x = nextafter(phi, -1.0e300);
-    return x;
 }
 
 // FP64 positions of buffer a from its fixed-point positions
@@ -560,9 +625,9 @@ __global__ void k_list_to_fp64(const DevState S, int a)
     if (i < n) {
         const FxGeom &F = S.fxg[col];
         const int4 h = S.fxh[a][i];
-        S.x[a][i] = from_fx(fx_join((unsigned)h.x, S.fxl[a][i]), F.o[0], F.u[0], F.per[0], F.phi[0]);
-        S.y[a][i] = from_fx(fx_join((unsigned)h.y, S.fxl[a][n + i]), F.o[1], F.u[1], F.per[1], F.phi[1]);
-        S.z[a][i] = from_fx(fx_join((unsigned)h.z, S.fxl[a][2 * (size_t)n + i]), F.o[2], F.u[2], F.per[2], F.phi[2]);
+        S.x[a][i] = from_fx(fx_join((unsigned)h.x, S.fxl[a][i]), F, 0);
+        S.y[a][i] = from_fx(fx_join((unsigned)h.y, S.fxl[a][n + i]), F, 1);
+        S.z[a][i] = from_fx(fx_join((unsigned)h.z, S.fxl[a][2 * (size_t)n + i]), F, 2);
     }
 }
 
