@@ -54,6 +54,11 @@ def parse():
     ap.add_argument("--only-main", action="store_true",
                     help="the timed steps and the roofline leg only (no other form, end-to-end, adjoint, "
                          "division or CPU legs): the run profiles capture")
+    ap.add_argument("--eager", action="store_true",
+                    help="with --only-main: every step launched kernel by kernel (profiling mode) from the start, "
+                         "so a profiler sees the first list build as the first build launch")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="print only the differentiation form's cost on its configuration (20 000 spheres, 200 steps)")
     ap.add_argument("--only-split", action="store_true",
                     help="print only the cell-division measurements (2 731 333 records, YEAST and FUNGI)")
     return ap.parse_args()
@@ -286,6 +291,52 @@ def split_cost(n, seed, reps=10, frac=0.05, fungi=False):
                              "seed": last_seed, "same_count_as_gpu": bool(kc == k)}}
 
 
+def host_link(nbytes=1 << 30, reps=3):
+    """Pinned host <-> device copy rate of this machine: one 1 GiB copy each way
+    alone, then both directions at once on two streams (best of reps, CUDA
+    events).  The end-to-end leg's copies are held against these."""
+    import torch
+    h1 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d1 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def h2d():
+        d1.copy_(h1, non_blocking=True)
+
+    def d2h():
+        h2.copy_(d2, non_blocking=True)
+
+    def both():
+        cur = torch.cuda.current_stream()
+        s1.wait_stream(cur)
+        s2.wait_stream(cur)
+        with torch.cuda.stream(s1):
+            d1.copy_(h1, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+
+    out = {}
+    for name, fn, nb in (("h2d", h2d, nbytes), ("d2h", d2h, nbytes), ("both", both, 2 * nbytes)):
+        best_ms = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1)
+            best_ms = t if best_ms is None else min(best_ms, t)
+        out[name + "_gbs"] = nb / (best_ms * 1e-3) / 1e9
+    del h1, h2, d1, d2
+    return out
+
+
 def sample_colonies(w, target):
     """Colonies of the workload whose sizes follow its colony-size mix: every
     k-th colony in order of size (stratified), k chosen so that the sample
@@ -441,6 +492,8 @@ def run_ours(args):
             tot += e0.elapsed_time(e1)
         return tot
 
+    if args.eager and args.only_main:
+        ctx.set_profiling(True)
     # warm-up, then the timed K steps
     timed_steps(prec, max(args.warmup, 3))
     if world > 1:
@@ -469,6 +522,25 @@ def run_ours(args):
     st = ctx.stats()
     ctx.set_profiling(False)
     k_ms = st["main_kernel_ms"] / max(st["main_kernel_launches"], 1)
+    # the force error of the kernel the timed steps ran: one more step of this
+    # trajectory (a list step where the list path runs) against an FP64 step
+    # from the same positions (the FP64 GPU step is bit-exact to the oracle)
+    Ps = w.particles.copy()
+    ctx.get_state(Ps, ("x", "y", "z") + (("theta", "phi") if kind == "rod" else ()))
+    r0 = ctx.stats()["n_rebins"]
+    ctx.step(w.dt, 1, prec)
+    V32 = w.particles.copy()
+    ctx.get_state(V32, ("velx", "vely", "velz"))
+    step_was_list = kind == "sphere" and prec == BMXG_FP32F and ctx.stats()["n_rebins"] - r0 <= 1 and list_mode
+    ref_ctx = Context(w.params, w.geoms)
+    ref_ctx.set_state(Ps, w.offsets)
+    ref_ctx.step(w.dt, 1, BMXG_FP64)
+    V64 = w.particles.copy()
+    ref_ctx.get_state(V64, ("velx", "vely", "velz"))
+    ref_ctx.close()
+    v32 = np.stack([V32["velx"], V32["vely"], V32["velz"]])
+    v64 = np.stack([V64["velx"], V64["vely"], V64["velz"]])
+    traj_err = float(np.abs(v32 - v64).max() / np.abs(v64).max())
     alg = ALG_BYTES[(kind, 1 if prec == BMXG_FP32F else 0)] * N
     peak, peak_kind = measured_peak()
     achieved = alg / (k_ms / 1e3) / 1e9
@@ -510,7 +582,7 @@ def run_ours(args):
     ctx.get_state(B, fields)
     va = np.stack([A["velx"], A["vely"], A["velz"]])
     vb = np.stack([B["velx"], B["vely"], B["velz"]])
-    rel_err = float(np.abs(va - vb).max() / np.abs(va).max())
+    rel_err_first = float(np.abs(va - vb).max() / np.abs(va).max())
 
     # end to end through the C ABI with pinned host buffers
     fin = ("x", "y", "z", "radius", "cell_type")
@@ -534,7 +606,22 @@ def run_ours(args):
     te = time.perf_counter() - t0
     e2e = {"value": N * world * ke / te, "unit": UNIT,
            "h2d_bytes_per_step": int(H.nbytes(fin)), "d2h_bytes_per_step": int(H.nbytes(fout)),
-           "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)"}
+           "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)",
+           "note": "a caller loading back the state it stored keeps the device's slot order and list"}
+    # the same calls when every load differs from the stored state (as after
+    # split_particles and ParticleExchange in bmx::Evolve): one particle moved
+    # by one ulp each call, so each load re-sorts and the step runs the
+    # per-step path
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(ke):
+        H["x"][it % N] = np.nextafter(H["x"][it % N], 1.0)
+        ctx.set_state(H, w.offsets, fields=fin)
+        ctx.step(w.dt, 1, prec)
+        ctx.get_state(H, fout)
+    tc = time.perf_counter() - t0
+    e2e_changed = {"value": N * world * ke / tc, "unit": UNIT, "steps": ke, "ms_per_call": 1e3 * tc / ke,
+                   "path": "the e2e calls with a changed state every call (full load)"}
 
     adj = None
     split = None
@@ -570,7 +657,15 @@ def run_ours(args):
                 "other_form": {"form": "FP64" if other == BMXG_FP64 else "FP32F", "value": v_other,
                                "unit": UNIT, "ms_per_step": ms_other / args.steps},
                 "fp32f_over_fp64": (value / v_other) if prec == BMXG_FP32F else (v_other / value),
-                "rel_force_err_fp32f_vs_fp64": rel_err}
+                "rel_force_err_fp32f_vs_fp64": traj_err,
+                "force_err": {"kernel": ("k_list_step" if step_was_list else kname),
+                              "how": "one more FP32F step at the end of the roofline leg's trajectory against an "
+                                     "FP64 step from the same positions; norm-wise relative velocity error",
+                              "value": traj_err,
+                              "first_step_after_load": {"kernel": "k_sphere<FP32F>" if kind == "sphere" else kname,
+                                                        "value": rel_err_first}},
+                "host_link": host_link(),
+                "e2e_changed_state": e2e_changed}
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -580,7 +675,14 @@ def run_ours(args):
 
 def main():
     args = parse()
-    if args.only_split:
+    if args.only_adjoint:
+        import torch
+        from boltzmannmfx_gb300 import Context, build, configs
+        from boltzmannmfx_gb300.abi import BMXG_FP64
+        build.build()
+        torch.cuda.set_device(0)
+        print(json.dumps(adjoint_cost(Context, configs, BMXG_FP64)), flush=True)
+    elif args.only_split:
         from boltzmannmfx_gb300 import build, configs
         build.build()
         print(json.dumps(split_cost(2731333, configs.SEED + 2)), flush=True)

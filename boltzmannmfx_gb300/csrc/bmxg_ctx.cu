@@ -655,7 +655,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         AL(S.clen, n); AL(S.area, n); AL(S.bscale, n);
         for (int k = 0; k < 2; ++k) { AL(S.theta[k], n); AL(S.phi[k], n); AL(S.trig[k], n); AL(S.tab[k], 13 * n); }
         AL(S.id, n); AL(S.cpu, n); AL(S.fuse_tip, n); AL(S.position, n); AL(S.fix_site, n);
-        AL(S.fflag, n); AL(S.sflag, n); AL(S.nflag, n); AL(S.dltd, 6 * n); AL(S.fc, 6 * n);
+        AL(S.fflag, n); AL(S.sflag, n); AL(S.nflag, n); AL(S.dltd, 6 * n); AL(S.fc, 6 * n); AL(S.axf, n);
     }
     }  // !reuse
 #undef AL

@@ -91,6 +91,7 @@ struct DevState {
     int *position, *fix_site, *fflag, *sflag, *nflag;
     int *dltd;         // 6 planes
     double *fc;        // 6 planes, force gather of the rod path
+    float4 *axf;       // per segment, this step: FP32 axis (nx, ny, nz) and length (k_rod_book)
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
     int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry: the

@@ -198,6 +198,34 @@ __device__ __forceinline__ double sep64(const DevState &S, const DevGeom &G, int
     return d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
 }
 
+// The interaction gate r^2 <= (r_lm - 1e-15)^2 (and BMXCheckPair's
+// r^2 <= neighborhood) decided from the FP32 bin offsets where they settle it:
+// the offsets are the FP64 differences rounded once, so the FP32 separation
+// is within ~1e-9 cm of the exact one, and a pair more than 1e-5 r_lm from
+// the gate is decided without FP64 arithmetic; the others take the exact
+// FP64 test.  Returns the decision and the FP32 separation r12f.
+__device__ __forceinline__ bool rod_gate(const DevState &S, const DevGeom &G, const DevParams &P, int a, int j,
+                                         int dxs, int dys, int dzs, int sx, int sy, float4 me, float Lif, float Ljf,
+                                         double xi, double yi, double zi, double Li, float *r12f)
+{
+    const float4 q = __ldg(&S.rel[a][j]);
+    r12f[0] = (me.x - q.x) - (float)dxs * G.dxf[0];
+    r12f[1] = (me.y - q.y) - (float)dys * G.dxf[1];
+    r12f[2] = (me.z - q.z) - (float)dzs * G.dxf[2];
+    const float r2f = r12f[0] * r12f[0] + r12f[1] * r12f[1] + r12f[2] * r12f[2];
+    if (G.nbh_trivial) {
+        const float rlmf = 1.5f * (Lif + Ljf) + P.bw32;
+        const float lo = rlmf * (1.0f - 1.0e-5f), hi = rlmf * (1.0f + 1.0e-5f);
+        if (r2f <= lo * lo) return true;
+        if (r2f > hi * hi) return false;
+    }
+    double d[3];
+    const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+    if (!G.nbh_trivial && !(r2 <= P.nbh)) return false;
+    const double rlm = 1.5 * (Li + S.clen[j]) + P.bw;
+    return r2 <= (rlm - kSmall) * (rlm - kSmall);
+}
+
 // ---- bookkeeping ----------------------------------------------------------
 __global__ void k_rod_book(const DevState S, const DevParams P, int a)
 {
@@ -209,24 +237,28 @@ __global__ void k_rod_book(const DevState S, const DevParams P, int a)
         S.nflag[i] = 0;
         int tb[13];
         for (int k = 0; k < 13; ++k) tb[k] = S.tab[a][(size_t)k * n + i];
+        {   // this step's FP32 axis and length, for the FP32F force kernel
+            const double4_32a tr = S.trig[a][i];
+            S.axf[i] = make_float4(d2f_rn(tr.y * tr.z), d2f_rn(tr.y * tr.w), d2f_rn(tr.x), d2f_rn(S.clen[i]));
+        }
         if (S.ctype[i] == kFungi) {
             const DevGeom &G = geom_of(S, i);
             int bx, by;
             col_to_bxy(G, S.col[a][i], bx, by);
             const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
             const double Li = S.clen[i];
+            const float Lif = d2f_rn(Li);
+            const float4 me = S.rel[a][i];
             const int iid = S.id[i], icpu = S.cpu[i];
             const int fs = S.fix_site[i];
             int pos = S.position[i];
             bool any = false;
             int rep = 0;
-            visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+            visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
                 if (S.ctype[j] != kFungi) return;
-                double d[3];
-                const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
-                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
-                const double rlm = 1.5 * (Li + S.clen[j]) + P.bw;
-                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
+                float r12f[3];
+                if (!rod_gate(S, G, P, a, j, dxs, dys, dzs, sx, sy, me, Lif, d2f_rn(S.clen[j]), xi, yi, zi, Li, r12f))
+                    return;
                 any = true;
                 const int jid = S.id[j], jcpu = S.cpu[j];
                 // position fix-up (bmx_cell_interaction_K.H:338-362); the
@@ -307,15 +339,15 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
             int tb[13];
             for (int k = 0; k < 13; ++k) tb[k] = S.tab[b][(size_t)k * n + i];
             const float4 me = S.rel[a][i];
+            const float4 axi = S.axf[i];  // FP32 axis and length (k_rod_book)
             double Sv[3] = {0.0, 0.0, 0.0}, Dv[3] = {0.0, 0.0, 0.0};
+            float Svf[3] = {0.0f, 0.0f, 0.0f}, Dvf[3] = {0.0f, 0.0f, 0.0f};  // the FP32F pairs' sums
             visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
                 if (S.ctype[j] != kFungi) return;
-                double d[3];
-                const double r2 = sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
-                if (!G.nbh_trivial && !(r2 <= P.nbh)) return;
+                const float4 axj = __ldg(&S.axf[j]);
+                float r12f[3];
+                if (!rod_gate(S, G, P, a, j, dxs, dys, dzs, sx, sy, me, axi.w, axj.w, xi, yi, zi, Li, r12f)) return;
                 const double Lj = S.clen[j];
-                const double rlm = 1.5 * (Li + Lj) + P.bw;
-                if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
                 // bonds: mutual entries in both (repaired) tables
                 int si = 0, sj = 0;
                 double kb = P.k_bond;
@@ -329,49 +361,50 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                         if ((itip > 0 && itip == si) || (jtip > 0 && jtip == sj)) kb = bsi * S.bscale[j] * kb;
                     }
                 }
-                const double4_32a trj = S.trig[a][j];
-                const double rS = ri + S.rad[j];
-                const double rA = rS + P.bw;
-                double f1[3], f2[3];
-                bool done = false;
                 if (PREC == BMXG_FP32F_FORM) {
-                    const float4 q = __ldg(&S.rel[a][j]);
-                    const float r12f[3] = {(me.x - q.x) - (float)dxs * G.dxf[0],
-                                           (me.y - q.y) - (float)dys * G.dxf[1],
-                                           (me.z - q.z) - (float)dzs * G.dxf[2]};
-                    const float nif[3] = {(float)ni[0], (float)ni[1], (float)ni[2]};
-                    const float njf[3] = {(float)(trj.y * trj.z), (float)(trj.y * trj.w), (float)trj.x};
-                    // near-parallel test: det of the closest-point system.  Bonded
-                    // pairs stay FP64: their spring acts on the difference of two
-                    // coincident end points, which FP32 end points would swamp
-                    // with rounding noise (k_bond x ulp of the segment length).
+                    // the pair in FP32 from the bin offsets and this step's FP32 axes,
+                    // except: bonded pairs (their spring acts on the difference of
+                    // two coincident end points, which FP32 end points would swamp
+                    // with rounding noise: k_bond x ulp of the segment length),
+                    // near-parallel segments (det < 0.05 Aii Ajj of the closest-point
+                    // system: the FP64 solve) and touching or crossing segments
+                    // (closest points within 1 % of the lengths: the direction of an
+                    // FP32 separation is end-point rounding noise there)
+                    const float nif[3] = {axi.x, axi.y, axi.z};
+                    const float njf[3] = {axj.x, axj.y, axj.z};
                     const float rij = nif[0] * njf[0] + nif[1] * njf[1] + nif[2] * njf[2];
                     const bool bonded = (si == 1 || si == 2) && (sj == 1 || sj == 2);
                     if (!bonded && 1.0f - rij * rij >= 0.05f) {
+                        const float rSf = me.w + __ldg(&S.rel[a][j]).w;
                         float g1[3], g2[3], rf;
-                        rod_site_forces<float>(r12f, nif, (float)Li, njf, (float)Lj, (float)rS, (float)rA,
-                                               (float)P.k, si, sj, (float)kb, g1, g2, &rf);
-                        // touching or crossing segments (closest points within 1 % of the
-                        // segment lengths): the direction of the FP32 separation is
-                        // rounding noise of the end points there, so such pairs go FP64
-                        if (rf >= 0.01f * (float)(Li + Lj)) {
+                        rod_site_forces<float>(r12f, nif, axi.w, njf, axj.w, rSf, rSf + P.bw32, P.k32, si, sj,
+                                               (float)kb, g1, g2, &rf);
+                        if (rf >= 0.01f * (axi.w + axj.w)) {
                             for (int k = 0; k < 3; ++k) {
-                                f1[k] = (double)g1[k];
-                                f2[k] = (double)g2[k];
+                                Svf[k] += g1[k] + g2[k];
+                                Dvf[k] += g1[k] - g2[k];
                             }
-                            done = true;
+                            return;
                         }
                     }
                 }
-                if (!done) {
-                    const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
-                    rod_site_forces<double>(d, ni, Li, nj, Lj, rS, rA, P.k, si, sj, kb, f1, f2);
-                }
+                double d[3];
+                sep64(S, G, a, j, sx, sy, xi, yi, zi, d);
+                const double4_32a trj = S.trig[a][j];
+                const double rS = ri + S.rad[j];
+                const double rA = rS + P.bw;
+                const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
+                double f1[3], f2[3];
+                rod_site_forces<double>(d, ni, Li, nj, Lj, rS, rA, P.k, si, sj, kb, f1, f2);
                 for (int k = 0; k < 3; ++k) {
                     Sv[k] += f1[k] + f2[k];
                     Dv[k] += f1[k] - f2[k];
                 }
             });
+            for (int k = 0; k < 3; ++k) {
+                Sv[k] += (double)Svf[k];
+                Dv[k] += (double)Dvf[k];
+            }
             // mobility of segment i (bmx_cell_interaction_K.H:812-840)
             const double area = S.area[i] / 2.0;
             const double arad = sqrt(area / (4.0 * kPi));
