@@ -484,6 +484,11 @@ int bmxg_set_params(bmxg_ctx *ctx, const bmxg_params *params)
                            cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->d_fxg, ctx->h_fxg.data(), sizeof(FxGeom) * ctx->ncol, cudaMemcpyHostToDevice,
                            ctx->stream));
+        if (ctx->S.has_rods && ctx->n) {  // the segment mobilities depend on the viscosity
+            const int blk = ctx->sh_misc.block, grd = grid_for(ctx, ctx->sh_misc, ctx->n);
+            launch_rod_mobility(ctx->S, dev_params(ctx->prm), grd, blk, ctx->stream);
+            CK(cudaGetLastError());
+        }
         CK(cudaStreamSynchronize(ctx->stream));
     }
     return BMXG_OK;
@@ -655,7 +660,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         AL(S.clen, n); AL(S.area, n); AL(S.bscale, n);
         for (int k = 0; k < 2; ++k) { AL(S.theta[k], n); AL(S.phi[k], n); AL(S.trig[k], n); AL(S.tab[k], 13 * n); }
         AL(S.id, n); AL(S.cpu, n); AL(S.fuse_tip, n); AL(S.position, n); AL(S.fix_site, n);
-        AL(S.fflag, n); AL(S.sflag, n); AL(S.nflag, n); AL(S.dltd, 6 * n); AL(S.fc, 6 * n); AL(S.axf, n);
+        AL(S.fflag, n); AL(S.sflag, n); AL(S.nflag, n); AL(S.dltd, 6 * n); AL(S.fc, 6 * n); AL(S.axf, n); AL(S.mob, n);
     }
     }  // !reuse
 #undef AL
@@ -744,6 +749,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         if ((rc = up_i(p->seg_id2, S.tab[0] + 5 * n, 4, 0))) return rc;
         if ((rc = up_i(p->site, S.tab[0] + 9 * n, 4, 0))) return rc;
         LAUNCH(launch_trig(S, 0, grd, blk, st));
+        LAUNCH(launch_rod_mobility(S, dev_params(ctx->prm), grd, blk, st));
     }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
@@ -1079,9 +1085,15 @@ int enqueue_step(bmxg_ctx *ctx, double dt, int precision, int a, int resync)
         if (k1) cudaEventRecord(k1, st);
     } else {
         const int rg = grid_for(ctx, ctx->sh_rod, n);
-        LAUNCH(launch_rod_book(S, P, a, rg, ctx->sh_rod.block, st));
+        // FP32F: the flat pipeline over the pairs the bookkeeping records
+        const bool pipe = precision == BMXG_FP32F && S.rnb;
+        if (pipe) cudaMemsetAsync(S.rctl, 0, sizeof(RodCtl), st);
+        LAUNCH(launch_rod_book(S, P, a, pipe, rg, ctx->sh_rod.block, st));
         if (k0) cudaEventRecord(k0, st);
-        LAUNCH(launch_rod_force(S, P, a, precision, rg, ctx->sh_rod.block, st));
+        if (pipe)
+            LAUNCH(launch_rod_pairs(S, P, a, ctx->nsm, (int)n, st));
+        else
+            LAUNCH(launch_rod_force(S, P, a, precision, rg, ctx->sh_rod.block, st));
         if (k1) cudaEventRecord(k1, st);
         LAUNCH(launch_rod_update(S, dt, a, mgrd, mblk, st));
     }
@@ -1162,6 +1174,25 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
     if (ctx->list_on && ctx->pair_capture && !ctx->S.pcap) {
         int rc = dalloc(ctx, &ctx->S.pcap, (size_t)(kPairCap + 1) * ctx->n);
         if (rc) return rc;
+        drop_graphs(ctx);
+    }
+    if (ctx->S.has_rods && precision == BMXG_FP32F && !ctx->S.rnb) {  // the FP32F rod pipeline's buffers
+        const size_t n = (size_t)ctx->n;
+        int2 *nb = nullptr, *work = nullptr;
+        int *cnt = nullptr;
+        double *res = nullptr;
+        RodCtl *ctl = nullptr;
+        int rc = dalloc(ctx, &nb, n * kRodCap);
+        if (!rc) rc = dalloc(ctx, &cnt, n);
+        if (!rc) rc = dalloc(ctx, &res, n * kRodCap * 6);
+        if (!rc) rc = dalloc(ctx, &work, n * kRodCap);
+        if (!rc) rc = dalloc(ctx, &ctl, 1);
+        if (rc) return rc;
+        ctx->S.rnb = nb;
+        ctx->S.rcnt = cnt;
+        ctx->S.rres = res;
+        ctx->S.rwork = work;
+        ctx->S.rctl = ctl;
         drop_graphs(ctx);
     }
     CK(cudaEventRecord(ctx->ev0, ctx->stream));

@@ -48,6 +48,14 @@ constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffe
 constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
 constexpr int kListBuildBlock = 128; // k_list_build's block (one slot per thread)
 constexpr int kSphereBlock = 64;     // per-step sphere kernels' block (one slot per thread)
+constexpr int kRodCap = 32;          // gated pairs per segment the FP32F rod pipeline holds (more: the
+                                     // segment walks its stencil in the segment kernel)
+
+// Per-step counters of the FP32F rod pipeline (k_rod.cu).
+struct RodCtl {
+    int kmax;   // largest number of gated pairs of a segment (at most kRodCap)
+    int nwork;  // pairs queued for FP64
+};
 
 // Device pointers of one context.  [2] arrays are ping-pong buffers indexed
 // by the step parity a (read) / b = a ^ 1 (write).
@@ -92,6 +100,17 @@ struct DevState {
     int *dltd;         // 6 planes
     double *fc;        // 6 planes, force gather of the rod path
     float4 *axf;       // per segment, this step: FP32 axis (nx, ny, nz) and length (k_rod_book)
+    double4_32a *mob;  // per segment: mobility (d0 + db, da - db, (d0 - db) / 2, 0) of its area,
+                       // length and the viscosity (k_rod_mobility, on every state or parameter load)
+    // FP32F rod pipeline (null until the first FP32F rod step): the gated pairs
+    // of each segment in the reference's list order, kRodCap planes of n
+    // entries (j, stencil code: bin offsets dx, dy, dz + 1 as a base-3 number in
+    // bits 0-4, image shifts sx, sy + 1 in bits 5-8), written by k_rod_book
+    int2 *rnb;
+    int *rcnt;         // per segment: its gated pairs (may exceed kRodCap)
+    double *rres;      // 6 x kRodCap planes of n: each pair's f1 + f2 (0-2), f1 - f2 (3-5)
+    int2 *rwork;       // the pairs evaluated in FP64: (i, k | si << 8 | sj << 12)
+    RodCtl *rctl;
 
     // FP32F neighbour list with a skin (null unless the context is in list mode)
     int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry: the
@@ -185,7 +204,11 @@ int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, in
                      cudaStream_t st);
 
 // ---- rods and mixed states (k_rod.cu) ------------------------------------
-int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st);
+int launch_rod_mobility(const DevState &S, const DevParams &P, int grid, int block, cudaStream_t st);
+// list: also record each segment's gated pairs (the FP32F pipeline)
+int launch_rod_book(const DevState &S, const DevParams &P, int a, bool list, int grid, int block, cudaStream_t st);
+// the FP32F pipeline after the bookkeeping: FP32 pairs, FP64 pairs, per-segment sums
+int launch_rod_pairs(const DevState &S, const DevParams &P, int a, int nsm, int n, cudaStream_t st);
 int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
                       cudaStream_t st);
 int launch_rod_update(const DevState &S, double dt, int a, int grid, int block, cudaStream_t st);

@@ -177,6 +177,20 @@ __device__ __forceinline__ int find_in_table(const int *tb, int id, int cpu)
     return -1;
 }
 
+// The site of the first entry of a register-held table tb (n_bnds, ids[4],
+// cpus[4], sites[4]) that names (id, cpu), or 0: the same answer as
+// tb[9 + find_in_table(...)], by selects over constant indices so the table
+// never goes to local memory.
+__device__ __forceinline__ int table_site(const int *tb, int id, int cpu)
+{
+    const int nb = min(tb[0], 4);
+    int site = 0;
+#pragma unroll
+    for (int k = 3; k >= 0; --k)
+        if (k < nb && tb[1 + k] == id && tb[5 + k] == cpu) site = tb[9 + k];
+    return site;
+}
+
 __device__ __forceinline__ int find_in_plane_table(const int *tab, int n, int j, int id, int cpu)
 {
     const int nb = min(__ldg(&tab[j]), 4);
@@ -227,11 +241,15 @@ __device__ __forceinline__ bool rod_gate(const DevState &S, const DevGeom &G, co
 }
 
 // ---- bookkeeping ----------------------------------------------------------
+// LIST: also record the segment's gated pairs, in the order of its walk, for
+// the FP32F pipeline (rnb, rcnt; the step's largest count into rctl->kmax).
+template <bool LIST>
 __global__ void k_rod_book(const DevState S, const DevParams P, int a)
 {
     const int b = a ^ 1;
     const int n = S.n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int cnt = 0;
         S.fflag[i] = 0;  // flag resets of bmx_pc_interaction.cpp:178-180
         S.sflag[i] = 0;
         S.nflag[i] = 0;
@@ -260,6 +278,13 @@ __global__ void k_rod_book(const DevState S, const DevParams P, int a)
                 if (!rod_gate(S, G, P, a, j, dxs, dys, dzs, sx, sy, me, Lif, d2f_rn(S.clen[j]), xi, yi, zi, Li, r12f))
                     return;
                 any = true;
+                if (LIST) {
+                    if (cnt < kRodCap) {
+                        const int code = ((dxs + 1) * 9 + (dys + 1) * 3 + (dzs + 1)) | (((sx + 1) * 3 + (sy + 1)) << 5);
+                        S.rnb[(size_t)cnt * n + i] = make_int2(j, code);
+                    }
+                    ++cnt;
+                }
                 const int jid = S.id[j], jcpu = S.cpu[j];
                 // position fix-up (bmx_cell_interaction_K.H:338-362); the
                 // neighbour's position is only tested against TIP, which no
@@ -293,16 +318,104 @@ __global__ void k_rod_book(const DevState S, const DevParams P, int a)
             if (rep) atomicAdd(&S.cnt->bond_repairs, (unsigned long long)rep);
         }
         for (int k = 0; k < 13; ++k) S.tab[b][(size_t)k * n + i] = tb[k];
+        if (LIST) {
+            // the site of i that its repaired table bonds to each recorded
+            // neighbour (1 or 2, else 0) into bits 9-10
+            for (int k = 0; k < min(cnt, kRodCap); ++k) {
+                int2 &e = S.rnb[(size_t)k * n + i];
+                const int site = table_site(tb, S.id[e.x], S.cpu[e.x]);
+                e.y |= ((site == 1 || site == 2) ? site : 0) << 9;
+            }
+            S.rcnt[i] = cnt;
+            const unsigned m = __activemask();
+            const int w = __reduce_max_sync(m, min(cnt, kRodCap));
+            if ((threadIdx.x & 31) == __ffs(m) - 1 && w > 0) atomicMax(&S.rctl->kmax, w);
+        }
     }
 }
 
+// ---- per-segment mobility -----------------------------------------------------
+// Mobility of a segment from its area, length and the viscosity
+// (bmx_cell_interaction_K.H:812-840): d0 for the segment as a sphere of the
+// same area, da along and db across its axis.  Stored as the combinations the
+// force gather applies, (d0 + db, da - db, (d0 - db) / 2), each the FP64
+// expression the gather evaluated per step before; none of the inputs changes
+// during a step, so it runs when a state or the parameters load.
+__global__ void k_rod_mobility(const DevState S, const DevParams P)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        double4_32a m = make_trig(0.0, 0.0, 0.0, 0.0);
+        if (S.ctype[i] == kFungi) {
+            const double Li = S.clen[i];
+            const double area = S.area[i] / 2.0;
+            const double arad = sqrt(area / (4.0 * kPi));
+            const double d0 = 1.0 / (6.0 * kPi * arad * P.visc);
+            double da, db;
+            if (Li > 2.0 * arad) {
+                da = (Li * Li - 2.0 * arad * arad / 3.0) / (4.0 * kPi * pow(Li, 3.0) * P.visc);
+                db = (Li * Li + 2.0 * arad * arad / 3.0) / (8.0 * kPi * pow(Li, 3.0) * P.visc);
+            } else {
+                da = (1.0 - 3.0 * Li / (16.0 * arad)) / (6.0 * kPi * arad * P.visc);
+                db = (1.0 - 9.0 * Li / (32.0 * arad)) / (6.0 * kPi * arad * P.visc);
+            }
+            m = make_trig(d0 + db, da - db, 0.5 * (d0 - db), 0.0);
+        }
+        S.mob[i] = m;
+    }
+}
+
+// Velocity (acc[0..2]) and rotation (acc[3..5]) of a segment in FP32 from its
+// site-force sums Sv = sum f1 + f2 and Dv = sum f1 - f2, its mobility m and
+// the growth-surface force on its two sites (bmx_cell_interaction_K.H:812-882,
+// :1067-1281), the axis from ni and L instead of the difference of the two
+// site positions (which FP32 would round at the magnitude of the position);
+// dzc = centre height above the surface, rounded once from FP64.
+__device__ __forceinline__ void rod_velocity32(const float *ni, float L, const float *Sv, const float *Dv,
+                                               const double4_32a &m, float dzc, float rS, const DevParams &P,
+                                               float *acc)
+{
+    const float m0 = d2f_rn(m.x), m1 = d2f_rn(m.y), m2 = d2f_rn(m.z);
+    const float ns = ni[0] * Sv[0] + ni[1] * Sv[1] + ni[2] * Sv[2];
+    float ax[3];
+    for (int k = 0; k < 3; ++k) {
+        acc[k] = 0.5f * (m0 * Sv[k] + m1 * ns * ni[k]);
+        ax[k] = -ni[k] * L;  // site 1 minus site 2
+    }
+    acc[3] = m2 * (ax[1] * Dv[2] - ax[2] * Dv[1]);
+    acc[4] = m2 * (ax[2] * Dv[0] - ax[0] * Dv[2]);
+    acc[5] = m2 * (ax[0] * Dv[1] - ax[1] * Dv[0]);
+    const float h = 0.5f * ni[2] * L;
+    float w1[3] = {0.0f, 0.0f, wall_law32(dzc - h, rS, P.z_k32, P.z_bw32, P.z_g32)};
+    float w2[3] = {0.0f, 0.0f, wall_law32(dzc + h, rS, P.z_k32, P.z_bw32, P.z_g32)};
+    const float ra = sqrtf(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    const float un[3] = {ax[0] / ra, ax[1] / ra, ax[2] / ra};
+    const float fn = (w1[2] - w2[2]) * un[2];
+    float vw[3];
+    for (int k = 0; k < 3; ++k) {
+        w1[k] -= 0.5f * fn * un[k];
+        w2[k] += 0.5f * fn * un[k];
+        vw[k] = 0.5f * (w1[k] + w2[k]);
+    }
+    for (int k = 0; k < 3; ++k) {
+        w1[k] -= 0.5f * vw[k];
+        w2[k] -= 0.5f * vw[k];
+    }
+    acc[0] += vw[0];
+    acc[1] += vw[1];
+    acc[2] += vw[2];
+    acc[3] += 0.5f * ((ax[1] * w1[2] - ax[2] * w1[1]) - (ax[1] * w2[2] - ax[2] * w2[1]));
+    acc[4] += 0.5f * ((ax[2] * w1[0] - ax[0] * w1[2]) - (ax[2] * w2[0] - ax[0] * w2[2]));
+    acc[5] += 0.5f * ((ax[0] * w1[1] - ax[1] * w1[0]) - (ax[0] * w2[1] - ax[1] * w2[0]));
+}
+
 // ---- force gather ----------------------------------------------------------
+// The force gather of slot i by a walk of its stencil (fc, fix_site).
 template <int PREC>
-__global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevParams P, int a)
+__device__ __forceinline__ void rod_force_slot(const DevState &S, const DevParams &P, int a, int i)
 {
     const int b = a ^ 1;
     const int n = S.n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    {
         const DevGeom &G = geom_of(S, i);
         int bx, by;
         col_to_bxy(G, S.col[a][i], bx, by);
@@ -337,6 +450,7 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
             const int itip = S.fuse_tip[i];
             const double bsi = S.bscale[i];
             int tb[13];
+#pragma unroll
             for (int k = 0; k < 13; ++k) tb[k] = S.tab[b][(size_t)k * n + i];
             const float4 me = S.rel[a][i];
             const float4 axi = S.axf[i];  // FP32 axis and length (k_rod_book)
@@ -347,15 +461,14 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                 const float4 axj = __ldg(&S.axf[j]);
                 float r12f[3];
                 if (!rod_gate(S, G, P, a, j, dxs, dys, dzs, sx, sy, me, axi.w, axj.w, xi, yi, zi, Li, r12f)) return;
-                const double Lj = S.clen[j];
                 // bonds: mutual entries in both (repaired) tables
                 int si = 0, sj = 0;
                 double kb = P.k_bond;
-                const int ib = find_in_table(tb, S.id[j], S.cpu[j]);
-                if (ib >= 0) {
+                const int isite = table_site(tb, S.id[j], S.cpu[j]);
+                if (isite != 0) {  // (an entry of site 0 bonds nothing either way)
                     const int jb = find_in_plane_table(S.tab[b], n, j, iid, icpu);
                     if (jb >= 0) {
-                        si = tb[9 + ib];
+                        si = isite;
                         sj = __ldg(&S.tab[b][(size_t)(9 + jb) * n + j]);
                         const int jtip = S.fuse_tip[j];
                         if ((itip > 0 && itip == si) || (jtip > 0 && jtip == sj)) kb = bsi * S.bscale[j] * kb;
@@ -377,8 +490,9 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                     if (!bonded && 1.0f - rij * rij >= 0.05f) {
                         const float rSf = me.w + __ldg(&S.rel[a][j]).w;
                         float g1[3], g2[3], rf;
+                        // (not bonded: the spring constant is not used)
                         rod_site_forces<float>(r12f, nif, axi.w, njf, axj.w, rSf, rSf + P.bw32, P.k32, si, sj,
-                                               (float)kb, g1, g2, &rf);
+                                               0.0f, g1, g2, &rf);
                         if (rf >= 0.01f * (axi.w + axj.w)) {
                             for (int k = 0; k < 3; ++k) {
                                 Svf[k] += g1[k] + g2[k];
@@ -395,35 +509,36 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
                 const double rA = rS + P.bw;
                 const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
                 double f1[3], f2[3];
-                rod_site_forces<double>(d, ni, Li, nj, Lj, rS, rA, P.k, si, sj, kb, f1, f2);
+                rod_site_forces<double>(d, ni, Li, nj, S.clen[j], rS, rA, P.k, si, sj, kb, f1, f2);
                 for (int k = 0; k < 3; ++k) {
                     Sv[k] += f1[k] + f2[k];
                     Dv[k] += f1[k] - f2[k];
                 }
             });
-            for (int k = 0; k < 3; ++k) {
-                Sv[k] += (double)Svf[k];
-                Dv[k] += (double)Dvf[k];
-            }
-            // mobility of segment i (bmx_cell_interaction_K.H:812-840)
-            const double area = S.area[i] / 2.0;
-            const double arad = sqrt(area / (4.0 * kPi));
-            const double d0 = 1.0 / (6.0 * kPi * arad * P.visc);
-            double da, db;
-            if (Li > 2.0 * arad) {
-                da = (Li * Li - 2.0 * arad * arad / 3.0) / (4.0 * kPi * pow(Li, 3.0) * P.visc);
-                db = (Li * Li + 2.0 * arad * arad / 3.0) / (8.0 * kPi * pow(Li, 3.0) * P.visc);
-            } else {
-                da = (1.0 - 3.0 * Li / (16.0 * arad)) / (6.0 * kPi * arad * P.visc);
-                db = (1.0 - 9.0 * Li / (32.0 * arad)) / (6.0 * kPi * arad * P.visc);
+            // mobility of segment i (bmx_cell_interaction_K.H:812-840), k_rod_mobility
+            const double4_32a mb = S.mob[i];
+            if (PREC == BMXG_FP32F_FORM) {
+                // the FP64 pairs' sums plus the FP32 pairs' (exactly converted), rounded
+                // once; velocity, rotation and the surface force in FP32
+                float sv[3], dv[3], af[6];
+                for (int k = 0; k < 3; ++k) {
+                    sv[k] = d2f_rn(Sv[k] + f2d_int(Svf[k]));
+                    dv[k] = d2f_rn(Dv[k] + f2d_int(Dvf[k]));
+                }
+                const float nif[3] = {axi.x, axi.y, axi.z};
+                rod_velocity32(nif, axi.w, sv, dv, mb, d2f_rn(zi - P.z_wall), me.w, P, af);
+                for (int k = 0; k < 6; ++k) acc[k] = f2d_int(af[k]);
+                S.fix_site[i] = 0;  // evaluateSurfaceForce (bmx_cell_interaction_K.H:1060)
+                for (int c = 0; c < 6; ++c) S.fc[(size_t)c * n + i] = acc[c];
+                return;
             }
             const double ns = ni[0] * Sv[0] + ni[1] * Sv[1] + ni[2] * Sv[2];
             double rv[3];
             for (int k = 0; k < 3; ++k) {
-                acc[k] = 0.5 * ((d0 + db) * Sv[k] + (da - db) * ns * ni[k]);
+                acc[k] = 0.5 * (mb.x * Sv[k] + mb.y * ns * ni[k]);
                 rv[k] = (-0.5 * ni[k] * Li) - (0.5 * ni[k] * Li);  // site 1 minus site 2
             }
-            const double c = 0.5 * (d0 - db);
+            const double c = mb.z;
             acc[3] = c * (rv[1] * Dv[2] - rv[2] * Dv[1]);
             acc[4] = c * (rv[2] * Dv[0] - rv[0] * Dv[2]);
             acc[5] = c * (rv[0] * Dv[1] - rv[1] * Dv[0]);
@@ -465,6 +580,177 @@ __global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevPa
             S.fix_site[i] = 0;  // evaluateSurfaceForce (:1060)
         }
         for (int c = 0; c < 6; ++c) S.fc[(size_t)c * n + i] = acc[c];
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(128) k_rod_force(const DevState S, const DevParams P, int a)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x)
+        rod_force_slot<PREC>(S, P, a, i);
+}
+
+// ---- FP32F pipeline ---------------------------------------------------------
+// With every segment's gated pairs recorded by k_rod_book, the FP32F force
+// gather runs flat instead of one stencil walk per thread (whose lanes
+// diverge over pair counts and over the FP32 and FP64 paths):
+//   k_rod_pair32  one pair per thread (pair k of segment i); evaluates it in
+//                 FP32 where the FP32F form allows, else queues it;
+//   k_rod_pair64  the queued pairs, one per thread, in FP64 (full warps on
+//                 the FP64 pipe);
+//   k_rod_seg32   per segment: its pairs' f1 + f2 and f1 - f2 summed in FP64 in
+//                 list order, then mobility and surface force in FP32.
+// Each pair writes its own slot, so the sums do not depend on the order in
+// which the queue filled.
+
+__device__ __forceinline__ void decode_pair(int code, int &dxs, int &dys, int &dzs, int &sx, int &sy)
+{
+    const int c = code & 31, s = (code >> 5) & 15;
+    dxs = c / 9 - 1;
+    dys = (c / 3) % 3 - 1;
+    dzs = c % 3 - 1;
+    sx = s / 3 - 1;
+    sy = s % 3 - 1;
+}
+
+__device__ __forceinline__ void put_pair(const DevState &S, int i, int k, const double *sv, const double *dv)
+{
+    const size_t n = (size_t)S.n;
+    for (int c = 0; c < 3; ++c) {
+        S.rres[((size_t)c * kRodCap + k) * n + i] = sv[c];
+        S.rres[((size_t)(3 + c) * kRodCap + k) * n + i] = dv[c];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_rod_pair32(const DevState S, const DevParams P, int a)
+{
+    const int b = a ^ 1;
+    const int n = S.n;
+    const long long total = (long long)n * S.rctl->kmax;
+    const int lane = threadIdx.x & 31;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / n);
+        const int i = (int)(t - (long long)k * n);
+        bool q64 = false;
+        int si = 0, sj = 0;
+        if (k < S.rcnt[i]) {
+            const int2 e = S.rnb[(size_t)k * n + i];
+            const int j = e.x;
+            int dxs, dys, dzs, sx, sy;
+            decode_pair(e.y, dxs, dys, dzs, sx, sy);
+            const DevGeom &G = geom_of(S, i);
+            const float4 me = S.rel[a][i], q = __ldg(&S.rel[a][j]);
+            // the offsets of the gate (rod_gate), recomputed
+            float r12f[3] = {(me.x - q.x) - (float)dxs * G.dxf[0], (me.y - q.y) - (float)dys * G.dxf[1],
+                             (me.z - q.z) - (float)dzs * G.dxf[2]};
+            // bonded: i's repaired table names j (the site k_rod_book found) and
+            // j's names i
+            const int isite = (e.y >> 9) & 3;
+            if (isite) {
+                const int jb = find_in_plane_table(S.tab[b], n, j, S.id[i], S.cpu[i]);
+                if (jb >= 0) {
+                    const int s2 = __ldg(&S.tab[b][(size_t)(9 + jb) * n + j]);
+                    si = isite;
+                    sj = (s2 == 1 || s2 == 2) ? s2 : 0;
+                }
+            }
+            // FP32 unless bonded, near-parallel or touching (as rod_force_slot)
+            q64 = true;
+            const float4 axi = S.axf[i], axj = __ldg(&S.axf[j]);
+            const float nif[3] = {axi.x, axi.y, axi.z};
+            const float njf[3] = {axj.x, axj.y, axj.z};
+            const float rij = nif[0] * njf[0] + nif[1] * njf[1] + nif[2] * njf[2];
+            if (!(si && sj) && 1.0f - rij * rij >= 0.05f) {
+                const float rSf = me.w + q.w;
+                float g1[3], g2[3], rf;
+                rod_site_forces<float>(r12f, nif, axi.w, njf, axj.w, rSf, rSf + P.bw32, P.k32, 0, 0, 0.0f, g1, g2,
+                                       &rf);
+                if (rf >= 0.01f * (axi.w + axj.w)) {
+                    double sv[3], dv[3];
+                    for (int c = 0; c < 3; ++c) {
+                        sv[c] = f2d_int(g1[c] + g2[c]);
+                        dv[c] = f2d_int(g1[c] - g2[c]);
+                    }
+                    put_pair(S, i, k, sv, dv);
+                    q64 = false;
+                }
+            }
+        }
+        // queue the FP64 pairs, one atomic per warp
+        const unsigned am = __activemask();
+        const unsigned qm = __ballot_sync(am, q64);
+        if (qm) {
+            const int leader = __ffs(qm) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&S.rctl->nwork, __popc(qm));
+            base = __shfl_sync(am, base, leader);
+            if (q64) S.rwork[base + __popc(qm & ((1u << lane) - 1u))] = make_int2(i, k | (si << 8) | (sj << 12));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_rod_pair64(const DevState S, const DevParams P, int a)
+{
+    const int n = S.n;
+    const int nw = S.rctl->nwork;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
+        const int2 it = S.rwork[w];
+        const int i = it.x, k = it.y & 255, si = (it.y >> 8) & 15, sj = (it.y >> 12) & 15;
+        const int2 e = S.rnb[(size_t)k * n + i];
+        const int j = e.x;
+        int dxs, dys, dzs, sx, sy;
+        decode_pair(e.y, dxs, dys, dzs, sx, sy);
+        const DevGeom &G = geom_of(S, i);
+        double kb = P.k_bond;
+        if (si && sj) {  // fusing tips (bmx_cell_interaction_K.H:552-600)
+            const int itip = S.fuse_tip[i], jtip = S.fuse_tip[j];
+            if ((itip > 0 && itip == si) || (jtip > 0 && jtip == sj)) kb = S.bscale[i] * S.bscale[j] * kb;
+        }
+        double d[3];
+        sep64(S, G, a, j, sx, sy, S.x[a][i], S.y[a][i], S.z[a][i], d);
+        const double4_32a tri = S.trig[a][i], trj = S.trig[a][j];
+        const double ni[3] = {tri.y * tri.z, tri.y * tri.w, tri.x};
+        const double nj[3] = {trj.y * trj.z, trj.y * trj.w, trj.x};
+        const double rS = S.rad[i] + S.rad[j];
+        const double rA = rS + P.bw;
+        double f1[3], f2[3], sv[3], dv[3];
+        rod_site_forces<double>(d, ni, S.clen[i], nj, S.clen[j], rS, rA, P.k, si, sj, kb, f1, f2);
+        for (int c = 0; c < 3; ++c) {
+            sv[c] = f1[c] + f2[c];
+            dv[c] = f1[c] - f2[c];
+        }
+        put_pair(S, i, k, sv, dv);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_rod_seg32(const DevState S, const DevParams P, int a)
+{
+    const int n = S.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int cnt = S.rcnt[i];
+        if (S.ctype[i] != kFungi || cnt > kRodCap) {
+            // spheres of a mixed state, and a segment with more pairs than the
+            // lists hold: the walk
+            rod_force_slot<BMXG_FP32F_FORM>(S, P, a, i);
+            continue;
+        }
+        double Sv[3] = {0.0, 0.0, 0.0}, Dv[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < cnt; ++k)
+            for (int c = 0; c < 3; ++c) {
+                Sv[c] += S.rres[((size_t)c * kRodCap + k) * n + i];
+                Dv[c] += S.rres[((size_t)(3 + c) * kRodCap + k) * n + i];
+            }
+        const float4 axi = S.axf[i];
+        float sv[3], dv[3], af[6];
+        for (int c = 0; c < 3; ++c) {
+            sv[c] = d2f_rn(Sv[c]);
+            dv[c] = d2f_rn(Dv[c]);
+        }
+        const float nif[3] = {axi.x, axi.y, axi.z};
+        rod_velocity32(nif, axi.w, sv, dv, S.mob[i], d2f_rn(S.z[a][i] - P.z_wall), S.rel[a][i].w, P, af);
+        for (int c = 0; c < 6; ++c) S.fc[(size_t)c * n + i] = f2d_int(af[c]);
+        S.fix_site[i] = 0;  // evaluateSurfaceForce (bmx_cell_interaction_K.H:1060)
     }
 }
 
@@ -676,10 +962,27 @@ int launch_exchange(const DevState &S, const DevParams &P, int a, const double *
     return 1;
 }
 
-int launch_rod_book(const DevState &S, const DevParams &P, int a, int grid, int block, cudaStream_t st)
+int launch_rod_mobility(const DevState &S, const DevParams &P, int grid, int block, cudaStream_t st)
 {
-    k_rod_book<<<grid, block, 0, st>>>(S, P, a);
+    k_rod_mobility<<<grid, block, 0, st>>>(S, P);
     return 1;
+}
+
+int launch_rod_book(const DevState &S, const DevParams &P, int a, bool list, int grid, int block, cudaStream_t st)
+{
+    if (list)
+        k_rod_book<true><<<grid, block, 0, st>>>(S, P, a);
+    else
+        k_rod_book<false><<<grid, block, 0, st>>>(S, P, a);
+    return 1;
+}
+
+int launch_rod_pairs(const DevState &S, const DevParams &P, int a, int nsm, int n, cudaStream_t st)
+{
+    k_rod_pair32<<<nsm * 8, 256, 0, st>>>(S, P, a);
+    k_rod_pair64<<<nsm * 4, 128, 0, st>>>(S, P, a);
+    k_rod_seg32<<<(n + 127) / 128, 128, 0, st>>>(S, P, a);
+    return 3;
 }
 
 int launch_rod_force(const DevState &S, const DevParams &P, int a, int precision, int grid, int block,
