@@ -461,6 +461,7 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     ctx.set_state(w.particles, w.offsets)
     ctx.autotune(os.path.join(ROOT, "boltzmannmfx_gb300", "_build", "autotune.json"))
+    shapes = ctx.shapes()
     ctx.set_state(w.particles, w.offsets)
     state_bytes = N * (24 * 2 + 16 * 2 + 8 * 2 + 4 * 2 + 8 + 4 + 1 + 24)
     flush = state_bytes < 2 * L2_BYTES
@@ -558,6 +559,7 @@ def run_ours(args):
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": ms / args.steps, "roofline": roof,
                               "gpu_launches": int(launches), "list_builds": int(rebins),
+                              "launch_shapes": shapes,
                               "note": "--only-main: a profiling run, not a bench line"}), flush=True)
         ctx.close()
         if world > 1:
@@ -650,10 +652,13 @@ def run_ours(args):
                                     "steps": args.steps,
                                     "per_step": "k_list_decide + k_list_step",
                                     "per_build": "k_list_rebin, 3 scan kernels, k_list_scatter, k_list_canon, "
-                                                 "k_list_build (CUDA-graph conditional node)"}
+                                                 "k_list_build, k_list_xcount, 3 scan kernels, k_list_xcopy "
+                                                 "(CUDA-graph conditional node)"}
                                    if list_mode else
                                    {"kind": "per-step binning", "rebins": int(rebins), "steps": args.steps}),
                 "clocks": clk.summary(),
+                "launch_shapes": dict(shapes, source="bmxg_autotune (cache keyed by device, n, colony-size "
+                                                     "histogram)"),
                 "other_form": {"form": "FP64" if other == BMXG_FP64 else "FP32F", "value": v_other,
                                "unit": UNIT, "ms_per_step": ms_other / args.steps},
                 "fp32f_over_fp64": (value / v_other) if prec == BMXG_FP32F else (v_other / value),

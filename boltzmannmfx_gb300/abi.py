@@ -80,6 +80,13 @@ class Stats(C.Structure):
                 ("main_kernel_ms", C.c_double), ("last_step_ms", C.c_double)]
 
 
+class Shapes(C.Structure):
+    """bmxg_shapes: the launch shapes in use."""
+    _fields_ = [("sphere_block", C.c_int32 * 2), ("sphere_grid", C.c_int32 * 2),
+                ("list_step_block", C.c_int32), ("list_step_passes", C.c_int32),
+                ("list_build_block", C.c_int32), ("reserved", C.c_int32)]
+
+
 class SplitParams(C.Structure):
     """bmxg_split_params: parameters of the division step."""
     _fields_ = [("max_vol", C.c_double), ("overlap", C.c_double), ("max_len", C.c_double),

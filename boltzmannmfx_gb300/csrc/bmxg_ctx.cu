@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <string>
 #include <utility>
@@ -76,6 +77,9 @@ struct bmxg_ctx {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::map<GraphKey, int> graph_kernels;  // kernels per replay of each graph
     Shape sh_sphere[2], sh_rod, sh_misc;
+    // list path shapes (bmxg_autotune): k_list_step's block and passes per
+    // chunk (0: the launcher's rule), k_list_build's block
+    int ls_block = kListStepBlock, ls_passes = 0, lb_block = kListBuildBlock;
     bmxg_stats stats{};
     int64_t launches = 0;                   // kernels enqueued (graph nodes counted per replay)
     bool profiling = false;
@@ -947,13 +951,19 @@ int ensure_list(bmxg_ctx *ctx, float skin)
         int rc;
         if ((rc = dalloc(ctx, &S.nbr, (size_t)(kNbrCap - kNbrInline) * ctx->n))) return rc;
         if ((rc = dalloc(ctx, &S.lrec, ctx->n))) return rc;
+        const size_t ngroups = ((size_t)ctx->n + 31) / 32;
+        if ((rc = dalloc(ctx, &S.xcnt, ngroups))) return rc;
+        if ((rc = dalloc(ctx, &S.xoff, ngroups + 1))) return rc;
+        if ((rc = dalloc(ctx, &S.xlist, (size_t)(kNbrCap - kNbrInline) * ctx->n))) return rc;
         for (int k = 0; k < 2; ++k) {
             if ((rc = dalloc(ctx, &S.fxh[k], ctx->n))) return rc;
             if ((rc = dalloc(ctx, &S.fxl[k], 3 * (size_t)ctx->n))) return rc;
         }
         if ((rc = dalloc(ctx, &S.cellcnt, ctx->ncells_total))) return rc;
         if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
-        if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints((int)ctx->ncells_total)))) return rc;
+        // (the scratch serves the scan of the cell counts and that of the groups' entries)
+        const int nscan = (int)std::max<int64_t>(ctx->ncells_total, ((int64_t)ctx->n + 31) / 32);
+        if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints(nscan)))) return rc;
         if ((rc = dalloc(ctx, &S.lctl, 1))) return rc;
         S.ncells_total = (int)ctx->ncells_total;
         CK(cudaMemsetAsync(S.cellcnt, 0, sizeof(int) * ctx->ncells_total, ctx->stream));
@@ -1041,7 +1051,7 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
         CK(cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
         CK(cudaStreamBeginCaptureToGraph(ctx->body_stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                          cudaStreamCaptureModeRelaxed));
-        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->body_stream);
+        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->lb_block, ctx->body_stream);
         const cudaError_t e1 = cudaPeekAtLastError();
         cudaGraph_t body = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(ctx->body_stream, &body);
@@ -1050,14 +1060,14 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
                         std::string("list build capture: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     } else {
         LAUNCH(launch_list_decide(S, 0, 0, st));
-        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, st);
+        launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->lb_block, st);
         const cudaError_t e = cudaPeekAtLastError();
         if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("list build: ") + cudaGetErrorString(e));
     }
     cudaEvent_t k0, k1;
     prof_events(ctx, &k0, &k1);
     if (k0) cudaEventRecord(k0, st);
-    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, kListStepBlock, st));
+    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, ctx->ls_block, ctx->ls_passes, st));
     if (k1) cudaEventRecord(k1, st);
     return BMXG_OK;
 }
@@ -1509,57 +1519,95 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
         CK(cudaGetDeviceProperties(&prop, ctx->device));
         std::snprintf(devname, sizeof(devname), "%s", prop.name);
     }
-    char key[512];
-    // look the shape up in the cache
+    // the colony-size histogram (count per power-of-two size class) keys the
+    // cache with the device and the particle count
+    std::string hist;
+    {
+        int cls[64] = {0};
+        for (int c = 0; c < ctx->ncol; ++c) {
+            const int64_t m = ctx->offsets[c + 1] - ctx->offsets[c];
+            int k = 0;
+            while (k < 62 && (1LL << k) <= m) ++k;
+            ++cls[k];
+        }
+        for (int k = 0; k < 64; ++k)
+            if (cls[k]) hist += std::to_string(k) + ":" + std::to_string(cls[k]) + ",";
+    }
+    auto cache_read = [&]() {
+        std::string txt;
+        if (!cache_path) return txt;
+        FILE *f = std::fopen(cache_path, "r");
+        if (!f) return txt;
+        char buf[4096];
+        size_t r;
+        while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, r);
+        std::fclose(f);
+        return txt;
+    };
+    auto cache_add = [&](const char *entry) {
+        if (!cache_path) return;
+        std::string txt = cache_read();
+        const size_t close = txt.rfind('}');
+        if (close == std::string::npos || txt.find('"') == std::string::npos)
+            txt = std::string("{\n  ") + entry + "\n}\n";
+        else
+            txt = txt.substr(0, close) + ",\n  " + entry + "\n}\n";
+        FILE *f = std::fopen(cache_path, "w");
+        if (f) {
+            std::fwrite(txt.data(), 1, txt.size(), f);
+            std::fclose(f);
+        }
+    };
+    // time `reps` launches after `warm` untimed ones (ms for the reps)
+    auto timeit = [&](int warm, int reps, const std::function<int()> &launch, float *ms) -> int {
+        for (int w = 0; w < warm; ++w) ctx->launches += launch();
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        for (int r = 0; r < reps; ++r) ctx->launches += launch();
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        CK(cudaGetLastError());
+        CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+        return BMXG_OK;
+    };
+    char key[768];
+    char entry[1024];
+    const DevState &S = ctx->S;
+    const DevParams P = dev_params(ctx->prm);
+    // the per-step stencil kernels of both forms
     for (int prec = 0; prec < 2; ++prec) {
-        std::snprintf(key, sizeof(key), "\"%s|sphere|%d|n=%lld|ncol=%d\"", devname, prec, (long long)n, ctx->ncol);
-        bool hit = false;
-        if (cache_path) {
-            FILE *f = std::fopen(cache_path, "r");
-            if (f) {
-                std::string txt;
-                char buf[4096];
-                size_t r;
-                while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, r);
-                std::fclose(f);
-                size_t pos = txt.find(key);
-                int bb = 0, gg = 0;
-                if (pos != std::string::npos &&
-                    std::sscanf(txt.c_str() + pos + std::strlen(key), ": {\"block\": %d, \"grid\": %d}", &bb, &gg) == 2 &&
-                    bb > 0) {
-                    ctx->sh_sphere[prec].block = bb;
-                    ctx->sh_sphere[prec].grid = gg;
-                    hit = true;
-                }
+        std::snprintf(key, sizeof(key), "\"%s|sphere|%d|n=%lld|ncol=%d|h=%s\"", devname, prec, (long long)n,
+                      ctx->ncol, hist.c_str());
+        {
+            const std::string txt = cache_read();
+            const size_t pos = txt.find(key);
+            int bb = 0, gg = 0;
+            if (pos != std::string::npos &&
+                std::sscanf(txt.c_str() + pos + std::strlen(key), ": {\"block\": %d, \"grid\": %d}", &bb, &gg) == 2 &&
+                bb > 0) {
+                ctx->sh_sphere[prec].block = bb;
+                ctx->sh_sphere[prec].grid = gg;
+                continue;
             }
         }
-        if (hit) continue;
         // sweep: the kernel reads buffer a and writes buffer b, so repeated
         // launches leave the state as it was except for the column counters,
         // which are cleared afterwards
-        const DevState &S = ctx->S;
-        const DevParams P = dev_params(ctx->prm);
         float best = 1e30f;
         Shape bs = ctx->sh_sphere[prec];
         const int blocks[] = {64, 128, 256};  // k_sphere is compiled with __launch_bounds__(256)
         for (int blk : blocks) {
             for (int mult = 1; mult <= 64; mult *= 2) {  // up to one slot per thread
-                Shape s;
-                s.block = blk;
-                s.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
-                const int grd = grid_for(ctx, s, n);
-                for (int w = 0; w < 2; ++w)
-                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream, 0));
-                CK(cudaEventRecord(ctx->ev0, ctx->stream));
-                for (int r = 0; r < 5; ++r)
-                    LAUNCH(launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk, ctx->stream, 0));
-                CK(cudaEventRecord(ctx->ev1, ctx->stream));
-                CK(cudaEventSynchronize(ctx->ev1));
+                Shape sh;
+                sh.block = blk;
+                sh.grid = ctx->nsm * mult * std::max(1, 1024 / blk);
+                const int grd = grid_for(ctx, sh, n);
                 float ms = 0.0f;
-                CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                if (int rc = timeit(2, 5, [&]() { return launch_sphere_step(S, P, 0.0, ctx->parity, prec, grd, blk,
+                                                                            ctx->stream, 0); }, &ms))
+                    return rc;
                 if (ms < best) {
                     best = ms;
-                    bs = s;
+                    bs = sh;
                 }
             }
         }
@@ -1567,31 +1615,86 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
         CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         ctx->sh_sphere[prec] = bs;
-        if (cache_path) {
-            std::string txt;
-            FILE *f = std::fopen(cache_path, "r");
-            if (f) {
-                char buf[4096];
-                size_t r;
-                while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, r);
-                std::fclose(f);
+        std::snprintf(entry, sizeof(entry), "%s: {\"block\": %d, \"grid\": %d, \"ms_per_5\": %.4f}", key, bs.block,
+                      bs.grid, best);
+        cache_add(entry);
+    }
+    // the FP32F list path: k_list_step's block and passes per chunk,
+    // k_list_build's block
+    const float skin = ctx->list_mode ? list_skin(ctx) : 0.0f;
+    if (skin > 0.0f) {
+        std::snprintf(key, sizeof(key), "\"%s|list|n=%lld|ncol=%d|h=%s\"", devname, (long long)n, ctx->ncol,
+                      hist.c_str());
+        const std::string txt = cache_read();
+        const size_t pos = txt.find(key);
+        int sb = 0, sp = 0, bb = 0;
+        if (pos != std::string::npos &&
+            std::sscanf(txt.c_str() + pos + std::strlen(key),
+                        ": {\"step_block\": %d, \"step_passes\": %d, \"build_block\": %d", &sb, &sp, &bb) == 3 &&
+            sb > 0 && bb > 0) {
+            ctx->ls_block = sb;
+            ctx->ls_passes = sp;
+            ctx->lb_block = bb;
+        } else {
+            // a list built on the loaded positions; then the step launches read
+            // buffer a and write buffer b (dt = 0), and the build launches
+            // rewrite the same list: the loaded state is untouched, and the
+            // list path starts afresh at the next step (list_valid = false)
+            if (int rc = ensure_list(ctx, skin)) return rc;
+            cudaStream_t st = ctx->stream;
+            const int a = ctx->parity;
+            const int mblk = ctx->sh_misc.block, mgrd = grid_for(ctx, ctx->sh_misc, n);
+            LAUNCH(launch_list_decide(S, 0, 0, st));
+            ctx->launches += launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->lb_block, st);
+            float best = 1e30f, best_b = 1e30f;
+            int best_sb = ctx->ls_block, best_sp = ctx->ls_passes, best_bb = ctx->lb_block;
+            for (int blk : {64, 128, 256}) {
+                for (int passes : {1, 2, 4}) {
+                    float ms = 0.0f;
+                    if (int rc = timeit(2, 5, [&]() { return launch_list_step(S, P, 0.0, a, ctx->nsm, blk, passes,
+                                                                                st); }, &ms))
+                        return rc;
+                    if (ms < best) {
+                        best = ms;
+                        best_sb = blk;
+                        best_sp = passes;
+                    }
+                }
+                float ms = 0.0f;
+                if (int rc = timeit(1, 3, [&]() { return launch_list_build(S, P, blk, st); }, &ms)) return rc;
+                if (ms < best_b) {
+                    best_b = ms;
+                    best_bb = blk;
+                }
             }
-            size_t close = txt.rfind('}');
-            char entry[768];
-            std::snprintf(entry, sizeof(entry), "%s: {\"block\": %d, \"grid\": %d, \"ms_per_5\": %.4f}", key,
-                          bs.block, bs.grid, best);
-            if (close == std::string::npos || txt.find('"') == std::string::npos)
-                txt = std::string("{\n  ") + entry + "\n}\n";
-            else
-                txt = txt.substr(0, close) + ",\n  " + entry + "\n}\n";
-            f = std::fopen(cache_path, "w");
-            if (f) {
-                std::fwrite(txt.data(), 1, txt.size(), f);
-                std::fclose(f);
-            }
+            CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
+            CK(cudaStreamSynchronize(st));
+            ctx->ls_block = best_sb;
+            ctx->ls_passes = best_sp;
+            ctx->lb_block = best_bb;
+            ctx->list_valid = false;
+            std::snprintf(entry, sizeof(entry),
+                          "%s: {\"step_block\": %d, \"step_passes\": %d, \"build_block\": %d, \"step_ms_per_5\": "
+                          "%.4f, \"build_ms_per_3\": %.4f}",
+                          key, best_sb, best_sp, best_bb, best, best_b);
+            cache_add(entry);
         }
     }
     drop_graphs(ctx);
+    return BMXG_OK;
+}
+
+int bmxg_get_shapes(const bmxg_ctx *ctx, bmxg_shapes *out)
+{
+    if (!ctx || !out) return BMXG_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    for (int k = 0; k < 2; ++k) {
+        out->sphere_block[k] = ctx->sh_sphere[k].block;
+        out->sphere_grid[k] = ctx->sh_sphere[k].grid;
+    }
+    out->list_step_block = ctx->ls_block;
+    out->list_step_passes = ctx->ls_passes;
+    out->list_build_block = ctx->lb_block;
     return BMXG_OK;
 }
 

@@ -45,8 +45,8 @@ constexpr int kNbrInline = 3;        // entries held in the slot's list record b
 constexpr int kNbrShift = 31;        // entries are slots below 2^31
 constexpr int kPairCap = 32;         // gated pairs per slot the step records when asked
 constexpr int kListBins = 0;         // list mode keeps its frozen bins in buffer 0
-constexpr int kListStepBlock = 128;  // k_list_step's block (12 per SM)
-constexpr int kListBuildBlock = 128; // k_list_build's block (one slot per thread)
+constexpr int kListStepBlock = 128;  // k_list_step's default block (at most 256; autotuned)
+constexpr int kListBuildBlock = 128; // k_list_build's default block (one slot per thread; at most 256)
 constexpr int kSphereBlock = 64;     // per-step sphere kernels' block (one slot per thread)
 constexpr int kRodCap = 32;          // gated pairs per segment the FP32F rod pipeline holds (more: the
                                      // segment walks its stencil in the segment kernel)
@@ -116,8 +116,15 @@ struct DevState {
     int *nbr;          // entries kNbrInline.. kNbrCap-1, one plane of n per entry: the
                        // neighbour slot (periodic images need no code: the fixed-point
                        // difference is the minimum image)
-    int4 *lrec;        // per slot: x = list length (saturating at 255); y, z, w = the
-                       // first kNbrInline entries
+    int4 *lrec;        // per slot: x = list length (bits 0-7, saturating at 255) and the
+                       // slot's place in its group's run of xlist (bits 8-17); y, z, w =
+                       // the first kNbrInline entries
+    // the entries past the inline ones, compacted for the step: per group of
+    // 32 consecutive slots (one warp of k_list_step) the groups' entries lie
+    // together, slot by slot in list order, from xoff[group] on
+    int *xcnt;         // per group: its entries past the inline ones (then scanned into xoff)
+    int *xoff;
+    int *xlist;
     int4 *fxh[2];      // list path positions, ping-pong with x/y/z: high 32 bits of the
                        // 64-bit fixed-point x, y, z (FxGeom) and the FP32 radius bits --
                        // what a neighbour gathers
@@ -197,10 +204,13 @@ int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStrea
 // list bins, column lists, and the list itself
 // (returns the kernels it enqueues, kListBodyKernels)
 int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_scratch, int grid, int block,
-                        cudaStream_t st);
-constexpr int kListBodyKernels = 7;
+                        int build_block, cudaStream_t st);
+// the list build kernel alone (gated on lctl->rebuild), build_block threads per block
+int launch_list_build(const DevState &S, const DevParams &P, int build_block, cudaStream_t st);
+constexpr int kListBodyKernels = 12;
 // force + wall + update over the list, reading buffer a and writing buffer b
-int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block,
+// (grid = the SM count; passes of the block per chunk of slots, <= 0: a rule)
+int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
                      cudaStream_t st);
 
 // ---- rods and mixed states (k_rod.cu) ------------------------------------

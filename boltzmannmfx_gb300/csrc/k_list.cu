@@ -277,7 +277,7 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
 // keeps the neighbours closer than rA + skin on the exact fixed-point
 // differences of the high words (+ a slack of four units per component and
 // the FP32 rounding of the test), and its list length.
-__global__ void __launch_bounds__(kListBuildBlock) k_list_build(const DevState S, const DevParams P)
+__global__ void __launch_bounds__(256, 6) k_list_build(const DevState S, const DevParams P)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
@@ -338,15 +338,61 @@ struct PairRec {
     }
 };
 
+// Entries of slot i's list past the inline ones that the step takes from
+// the compacted list (none for a slot whose list overflowed: it walks).
+__device__ __forceinline__ int list_extra(int cnt)
+{
+    return (cnt > kNbrInline && cnt <= kNbrCap) ? cnt - kNbrInline : 0;
+}
+
+// Compaction of the list entries past the inline ones, per group of 32
+// consecutive slots (the step's warps): the groups' counts, then (after
+// their exclusive scan into xoff) each slot's entries copied from the
+// build's planes to xlist[xoff[group] + the entries of the group's earlier
+// slots].  One slot per thread, whole warps.
+__global__ void k_list_xcount(const DevState S)
+{
+    if (!S.lctl->rebuild) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = (i < S.n) ? list_extra(__ldg(&S.lrec[i].x) & 0xff) : 0;
+    const int t = __reduce_add_sync(0xffffffffu, x);
+    if ((threadIdx.x & 31) == 0 && i < S.n) S.xcnt[i >> 5] = t;
+}
+
+__global__ void k_list_xcopy(const DevState S)
+{
+    if (!S.lctl->rebuild) return;
+    const int n = S.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int x = (i < n) ? list_extra(S.lrec[i].x & 0xff) : 0;
+    int o = x;  // inclusive scan over the warp
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, o, d);
+        if (lane >= d) o += v;
+    }
+    if (x) {
+        int *dst = S.xlist + __ldg(&S.xoff[i >> 5]) + (o - x);
+        for (int k = 0; k < x; ++k) dst[k] = __ldg(&S.nbr[(size_t)k * n + i]);
+    }
+    // the slot's place in its group's run beside the list length (bits 8-17:
+    // at most 31 x 29 entries precede it)
+    if (i < n) S.lrec[i].x = (S.lrec[i].x & 0xff) | ((o - x) << 8);
+}
+
 // FP32F sphere step over the list: pair offsets from the fixed-point high
 // words, pair math and wall law in FP32, the increments added in 64-bit fixed
 // point (the periodic wrap is the unsigned wrap; the domain test of the
 // closed z axis compares the high word).
-// Each block takes a contiguous chunk of slots, so a thread's colony is
-// found by one binary search and then by stepping forward from the last one.
-// The list metadata and the first entries come in one 16-byte record.
+// Each block takes a contiguous chunk of slots (a multiple of 32), so a
+// thread's colony is found by one binary search and then by stepping forward
+// from the last one.  The list metadata and the first entries come in one
+// 16-byte record; the rest (a slot's list is mostly 0 to 3 long, rarely up to
+// a dozen) from the compacted list, where a warp's entries lie together: a
+// few sectors per warp, not one per entry as a plane per list position would
+// cost.
 template <bool CAP>
-__global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
+__global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
 {
     constexpr int B = kListBins;
     const int b = a ^ 1;
@@ -355,7 +401,6 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
     const float zkf = P.z_k32, zbwf = P.z_bw32, zgf = P.z_g32;
     const int4 *__restrict__ ga = S.fxh[a];
     const unsigned *__restrict__ la = S.fxl[a];
-    const int *__restrict__ nbr = S.nbr;
     // smallest and largest increment per component (order-preserving keys),
     // per warp in shared memory: reduced over the warp after each pass, so
     // that no register holds them through the list walk
@@ -371,41 +416,53 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
     int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.cbase, S.ncol, i0 + threadIdx.x) : 0;
     for (int base = i0; base < i1; base += blockDim.x) {  // same trip count for every thread
         const int i = base + threadIdx.x;
+        const bool act = i < i1;
         unsigned lo0 = kKeyPosInf, lo1 = kKeyPosInf, lo2 = kKeyPosInf;
         unsigned hi0 = kKeyNegInf, hi1 = kKeyNegInf, hi2 = kKeyNegInf;
-        if (i < i1) {
+        int4 h = make_int4(0, 0, 0, 0);
+        int cnt = 0;
+        float ux = 0.0f, uy = 0.0f, uz = 0.0f;
+        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+        PairRec pr{CAP ? S.pcap : nullptr, i, 0};
+        // the pair term: offset from the high words, the gate r < rA, F / r
+        auto term = [&](const int4 me, const int4 q, float tx, float ty, float tz, float &ex, float &ey, float &ez,
+                        float &Fi) -> bool {
+            ex = (float)(me.x - q.x) * tx;
+            ey = (float)(me.y - q.y) * ty;
+            ez = (float)(me.z - q.z) * tz;
+            const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+            const float rSf = __fadd_rn(__int_as_float(me.w), __int_as_float(q.w));
+            const float rAf = __fadd_rn(rSf, bwf);
+            if (!(r2f < __fmul_rn(rAf, rAf))) return false;
+            const float inv = rsqrtf(r2f);
+            const float rn = __fmul_rn(r2f, inv);
+            const float d1 = __fsub_rn(rn, rAf);
+            const float Fm = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
+            Fi = __fmul_rn(Fm, inv);
+            return true;
+        };
+        auto pair = [&](int j, const int4 q) {
+            float ex, ey, ez, Fi;
+            if (!term(h, q, ux, uy, uz, ex, ey, ez, Fi)) return;
+            if (CAP) pr.add(j);
+            gx = __fmaf_rn(Fi, ex, gx);
+            gy = __fmaf_rn(Fi, ey, gy);
+            gz = __fmaf_rn(Fi, ez, gz);
+        };
+        int4 rec = make_int4(0, 0, 0, 0);
+        if (act) {
             while (colony + 1 < S.ncol && __ldg(&S.cbase[colony + 1]) <= i) ++colony;
-            const FxGeom &F = S.fxg[colony];
-            const int4 rec = __ldg(&S.lrec[i]);
-            const int4 h = ga[i];
-            const int cnt = rec.x & 0xff;
-            const float4 fu = *reinterpret_cast<const float4 *>(F.uh);  // units and the growth surface
-            const float ux = fu.x, uy = fu.y, uz = fu.z;
-            const unsigned zw = __float_as_uint(fu.w);
-            const float ri = __int_as_float(h.w);
-            float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-            PairRec pr{CAP ? S.pcap : nullptr, i, 0};
-            auto pair = [&](int j, const int4 q) {
-                const float ex = (float)(h.x - q.x) * ux;
-                const float ey = (float)(h.y - q.y) * uy;
-                const float ez = (float)(h.z - q.z) * uz;
-                const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-                const float rSf = __fadd_rn(ri, __int_as_float(q.w));
-                const float rAf = __fadd_rn(rSf, bwf);
-                if (!(r2f < __fmul_rn(rAf, rAf))) return;
-                if (CAP) pr.add(j);
-                const float inv = rsqrtf(r2f);
-                const float rn = __fmul_rn(r2f, inv);
-                const float d1 = __fsub_rn(rn, rAf);
-                const float Fm = __fmul_rn(__fmul_rn(__fmul_rn(-kf, d1), d1), __fsub_rn(rn, rSf));
-                const float Fi = __fmul_rn(Fm, inv);
-                gx = __fmaf_rn(Fi, ex, gx);
-                gy = __fmaf_rn(Fi, ey, gy);
-                gz = __fmaf_rn(Fi, ez, gz);
-            };
+            rec = __ldg(&S.lrec[i]);
+            h = ga[i];
+            cnt = rec.x & 0xff;
+            const float4 fu = *reinterpret_cast<const float4 *>(S.fxg[colony].uh);
+            ux = fu.x;
+            uy = fu.y;
+            uz = fu.z;
+        }
+        if (act) {
             if (cnt <= kNbrCap) {
-                // the first entries came with the metadata: their gathers go out
-                // together, one round trip for the typical short list
+                // the inline entries: their gathers go out together
                 const int4 z4 = make_int4(0, 0, 0, 0);
                 const int4 p0 = (cnt > 0) ? __ldg(&ga[rec.y]) : z4;
                 const int4 p1 = (cnt > 1) ? __ldg(&ga[rec.z]) : z4;
@@ -413,27 +470,30 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
                 if (cnt > 0) pair(rec.y, p0);
                 if (cnt > 1) pair(rec.z, p1);
                 if (cnt > 2) pair(rec.w, p2);
-                const int *col = nbr + i;  // entry k in plane k - kNbrInline
-                int k = kNbrInline;
-                // four entries in flight at a time: the list loads and the
-                // neighbour gathers are independent across entries
-                for (; k + 4 <= cnt; k += 4) {
-                    const int e0 = __ldg(col + (size_t)(k - kNbrInline) * n);
-                    const int e1 = __ldg(col + (size_t)(k + 1 - kNbrInline) * n);
-                    const int e2 = __ldg(col + (size_t)(k + 2 - kNbrInline) * n);
-                    const int e3 = __ldg(col + (size_t)(k + 3 - kNbrInline) * n);
-                    const int4 q0 = __ldg(&ga[e0]);
-                    const int4 q1 = __ldg(&ga[e1]);
-                    const int4 q2 = __ldg(&ga[e2]);
-                    const int4 q3 = __ldg(&ga[e3]);
-                    pair(e0, q0);
-                    pair(e1, q1);
-                    pair(e2, q2);
-                    pair(e3, q3);
-                }
-                for (; k < cnt; ++k) {
-                    const int e = __ldg(col + (size_t)(k - kNbrInline) * n);
-                    pair(e, __ldg(&ga[e]));
+                // this slot's entries past the inline ones, from its place in
+                // its warp's run of the compacted list
+                const int xl = list_extra(cnt);
+                if (xl) {
+                    const int *xs = S.xlist + __ldg(&S.xoff[i >> 5]) + ((rec.x >> 8) & 0x3ff);
+                    int k = 0;
+                    // four entries in flight at a time: the list loads and the
+                    // neighbour gathers are independent across entries
+                    for (; k + 4 <= xl; k += 4) {
+                        const int e0 = __ldg(xs + k), e1 = __ldg(xs + k + 1);
+                        const int e2 = __ldg(xs + k + 2), e3 = __ldg(xs + k + 3);
+                        const int4 q0 = __ldg(&ga[e0]);
+                        const int4 q1 = __ldg(&ga[e1]);
+                        const int4 q2 = __ldg(&ga[e2]);
+                        const int4 q3 = __ldg(&ga[e3]);
+                        pair(e0, q0);
+                        pair(e1, q1);
+                        pair(e2, q2);
+                        pair(e3, q3);
+                    }
+                    for (; k < xl; ++k) {
+                        const int e = __ldg(xs + k);
+                        pair(e, __ldg(&ga[e]));
+                    }
                 }
             } else {  // list overflow: walk the build's cells with the current records
                 const DevGeom &G = S.geoms[colony];
@@ -444,7 +504,12 @@ __global__ void __launch_bounds__(kListStepBlock, 12) k_list_step(const DevState
                     pair(j, __ldg(&ga[j]));
                 });
             }
+        }
+        if (act) {
+            const FxGeom &F = S.fxg[colony];
             if (CAP) pr.done();
+            const unsigned zw = F.zw;
+            const float ri = __int_as_float(h.w);
             const float dzw = (float)(int)((unsigned)h.z - zw) * uz;
             const float vx = gx, vy = gy, vz = gz + wall_law32(dzw, ri, zkf, zbwf, zgf);
             const float ix = dtf * vx, iy = dtf * vy, iz = dtf * vz;
@@ -653,8 +718,14 @@ int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStrea
     return 1;
 }
 
+int launch_list_build(const DevState &S, const DevParams &P, int build_block, cudaStream_t st)
+{
+    k_list_build<<<(S.n + build_block - 1) / build_block, build_block, 0, st>>>(S, P);
+    return 1;
+}
+
 int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_scratch, int grid, int block,
-                        cudaStream_t st)
+                        int build_block, cudaStream_t st)
 {
     const int *gate = &S.lctl->rebuild;
     // one slot per thread (a block's colonies from one search)
@@ -663,24 +734,32 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     int k = 1 + launch_scan(S.cellcnt, S.cellstart, S.ncells_total, scan_scratch, st, gate);
     k_list_scatter<<<g1, block, 0, st>>>(S);
     k_list_canon<<<g1, block, 0, st>>>(S, a);
-    // the build: one slot per thread in 128-thread blocks (the stencil walks
+    // the build: one slot per thread in small blocks (the stencil walks
     // differ in length from slot to slot; small blocks on a grid of every
     // slot let the scheduler balance them)
-    k_list_build<<<(S.n + kListBuildBlock - 1) / kListBuildBlock, kListBuildBlock, 0, st>>>(S, P);
-    return k + 3;
+    launch_list_build(S, P, build_block, st);
+    // the entries past the inline ones, compacted per group of 32 slots
+    const int gx = (S.n + 127) / 128;
+    k_list_xcount<<<gx, 128, 0, st>>>(S);
+    k = k + launch_scan(S.xcnt, S.xoff, (S.n + 31) / 32, scan_scratch, st, gate);
+    k_list_xcopy<<<gx, 128, 0, st>>>(S);
+    return k + 5;
 }
 
-int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block,
+int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
                      cudaStream_t st)
 {
-    // two passes of the block per chunk: short enough that the block
-    // scheduler evens out the uneven list lengths of the colonies (one wave
-    // of long chunks ends on its slowest block), long enough to amortise the
-    // colony search and the block's reduction of the increment spreads.  One
-    // pass when two would leave fewer than four waves of twelve blocks per SM
-    // (grid = the SM count): small states need the blocks more.
-    const int two = (S.n + 2 * block - 1) / (2 * block);
-    const int chunk = (two >= 4 * 12 * grid) ? 2 * block : block;
+    // passes of the block per chunk (passes <= 0: the rule): short enough that
+    // the block scheduler evens out the uneven list lengths of the colonies
+    // (one wave of long chunks ends on its slowest block), long enough to
+    // amortise the colony search and the block's reduction of the increment
+    // spreads.  The rule: two, or one when two would leave fewer than four
+    // waves of 1536 threads per SM (grid = the SM count).
+    int chunk = block * passes;
+    if (passes <= 0) {
+        const int two = (S.n + 2 * block - 1) / (2 * block);
+        chunk = (two >= 4 * (1536 / block) * grid) ? 2 * block : block;
+    }
     const int nb = (S.n + chunk - 1) / chunk;
     if (S.pcap) k_list_step<true><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
     else k_list_step<false><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);

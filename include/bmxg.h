@@ -441,9 +441,25 @@ int  bmxg_get_step_pairs(bmxg_ctx *ctx, int64_t *offs, int32_t *idx, int64_t cap
 int  bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode);
 
 /* Time the launch shapes of the step kernels on the loaded state and keep
- * the fastest; results are cached in a JSON file at cache_path (may be NULL:
- * no cache). */
+ * the fastest: the per-step stencil kernels of both forms (block, grid) and,
+ * where the FP32F list path applies, the list step (block, passes of the
+ * block per chunk of slots) and the list build (block).  Results are cached
+ * in a JSON file at cache_path (may be NULL: no cache), keyed by the device,
+ * the particle count and the colony-size histogram.  The loaded state is left
+ * as it was.  The reference has no counterpart (AMReX tiles its loops by a
+ * fixed tile size, bmx_pc_interaction.cpp:111-114). */
 int  bmxg_autotune(bmxg_ctx *ctx, const char *cache_path);
+
+/* The launch shapes in use (defaults until bmxg_autotune picks others). */
+typedef struct bmxg_shapes {
+    int32_t sphere_block[2];    /* per-step stencil kernel, [FP64, FP32F]            */
+    int32_t sphere_grid[2];     /* 0: one slot per thread                            */
+    int32_t list_step_block;    /* FP32F list step                                   */
+    int32_t list_step_passes;   /* passes of the block per chunk (0: the size rule)  */
+    int32_t list_build_block;   /* list build                                        */
+    int32_t reserved;
+} bmxg_shapes;
+int  bmxg_get_shapes(const bmxg_ctx *ctx, bmxg_shapes *out);
 
 #ifdef __cplusplus
 }

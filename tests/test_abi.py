@@ -54,6 +54,7 @@ def test_struct_layout_matches_c(tmp_path):
         "bmxg_geometry": [f for f, _ in abi.Geometry._fields_],
         "bmxg_particles": [f for f, _ in abi.ParticlesStruct._fields_],
         "bmxg_stats": [f for f, _ in abi.Stats._fields_],
+        "bmxg_shapes": [f for f, _ in abi.Shapes._fields_],
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bmxg.h"', "int main(void){"]
     for st, fs in fields.items():
@@ -67,7 +68,8 @@ def test_struct_layout_matches_c(tmp_path):
     out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
                                                          check=True).stdout.split("\n") if l)
     for st, cls in (("bmxg_params", abi.Params), ("bmxg_geometry", abi.Geometry),
-                    ("bmxg_particles", abi.ParticlesStruct), ("bmxg_stats", abi.Stats)):
+                    ("bmxg_particles", abi.ParticlesStruct), ("bmxg_stats", abi.Stats),
+                    ("bmxg_shapes", abi.Shapes)):
         assert int(out[st]) == C.sizeof(cls), st
         for f, _ in cls._fields_:
             assert int(out[f"{st}.{f}"]) == getattr(cls, f).offset, (st, f)

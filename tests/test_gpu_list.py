@@ -96,9 +96,9 @@ def test_graph_and_eager_steps_agree(gpu_lib):
     sa = A.stats()
     B.step(w.dt, 24, BMXG_FP32F)
     sb = B.stats()
-    # two kernels per step, seven per build, and the list's set-up (the
+    # two kernels per step, twelve per build, and the list's set-up (the
     # fixed-point positions) once
-    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 7 * sa["n_rebins"] + 1
+    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 12 * sa["n_rebins"] + 1
     assert sa["n_rebins"] == sb["n_rebins"]
     QA, QB = read(A, w.particles), read(B, w.particles)
     for k in ("x", "y", "z", "velx", "vely", "velz"):
@@ -225,3 +225,32 @@ def test_per_step_position_accumulation_is_binary64(gpu_lib):
         inside = (want >= g.prob_lo[ax]) & (want < g.prob_hi[ax])  # not wrapped this step
         assert inside.mean() > 0.99
         assert np.array_equal(Q[k][inside], want[inside]), k
+
+
+def test_autotune_list_shapes_leave_state_and_steps_unchanged(gpu_lib, tmp_path):
+    """bmxg_autotune sweeps the list step's block and passes and the build's
+    block: it leaves the loaded state as it was, the steps after it are
+    bit-identical to those of an untuned context (each slot's arithmetic does
+    not depend on the launch shape), and a second context takes the shapes
+    from the cache."""
+    w = configs.colonies(ncol=12)
+    cache = str(tmp_path / "tune.json")
+    A, B = ctx_for(w), ctx_for(w)
+    A.autotune(cache)
+    sh = A.shapes()
+    assert sh["list_step_block"] in (64, 128, 256) and sh["list_step_passes"] in (1, 2, 4)
+    assert sh["list_build_block"] in (64, 128, 256)
+    Q0 = read(A, w.particles)
+    for k in ("x", "y", "z"):
+        assert np.array_equal(Q0[k], w.particles[k]), k
+    A.step(w.dt, 24, BMXG_FP32F)
+    B.step(w.dt, 24, BMXG_FP32F)
+    assert A.stats()["n_rebins"] == B.stats()["n_rebins"] >= 1
+    QA, QB = read(A, w.particles), read(B, w.particles)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(QA[k], QB[k]), k
+    C = ctx_for(w)
+    C.autotune(cache)
+    assert C.shapes() == sh
+    for c in (A, B, C):
+        c.close()
