@@ -49,64 +49,165 @@ __device__ __forceinline__ void walk(const DevState &S, const DevGeom &G, int a,
     }
 }
 
+// The FP64 pair term of slot i (at xi, yi, zi, radius ri, colony geometry
+// G) from neighbour j under image shift (sx, sy), in the reference's operation
+// order: false when the pair is not in the neighbour list or beyond the
+// cutoff, else the three products F u_x, F u_y, F u_z that the gather adds.
+__device__ __forceinline__ bool sphere_term64(const DevState &S, const DevGeom &G, const DevParams &P, int a,
+                                              double xi, double yi, double zi, double ri, int j, int sx, int sy,
+                                              double *t)
+{
+    const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
+    const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
+    const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (!G.nbh_trivial && !(r2 <= P.nbh)) return false;  // not in the neighbour list
+    const double rj = S.rad[j];
+    const double rlm = ri + rj + P.bw;                     // maxInteractionDistance
+    if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return false;
+    const double rS = ri + rj;
+    const double rA = rS + P.bw;
+    const double rn = sqrt(r2);
+    const double ux = dx / rn, uy = dy / rn, uz = dz / rn;
+    const double F = (rn < rA) ? -P.k * (rn - rA) * (rn - rA) * (rn - rS) : 0.0;
+    t[0] = F * ux;
+    t[1] = F * uy;
+    t[2] = F * uz;
+    return true;
+}
+
+// FP64 plain step.  Each lane walks its slot's stencil and screens the
+// candidates in FP32 (FP32 and integer work); the few that can pass the
+// cutoff (about 1.3 per slot on the colonies) are staged in shared memory,
+// and the warp then evaluates its slots' staged pairs together, one per lane,
+// so that the FP64 gate, square root and divisions run in full warps (GB300
+// issues FP64 at 2 lanes per clock per SM whatever the mask: a lane walking
+// its own candidates keeps 8 of 32 lanes busy in those instructions).  Each
+// slot then adds its pairs' terms in walk order -- the same FP64 values in
+// the same order as a walk that evaluates each pair when it meets it, so the
+// result stays bit-identical to the oracle.  A slot with more than kStage64
+// staged candidates evaluates them itself, in order, as it walks.
+constexpr int kStage64 = 8;
+
 template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)
 {
+    // per warp: the lanes' staged candidates (j, image code), then one round's
+    // terms (dynamic shared memory, sized by the launcher)
+    extern __shared__ unsigned char sm64[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int2 *stage = reinterpret_cast<int2 *>(sm64) + (size_t)w * 32 * kStage64;
+    double *term = reinterpret_cast<double *>(sm64 + (size_t)(blockDim.x >> 5) * 32 * kStage64 * sizeof(int2)) +
+                   (size_t)w * 3 * 32;
     const int b = a ^ 1;
     const float bwf = (float)P.bw;  // once per thread: a conversion is an FP64-pipe instruction
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-        const DevGeom &G = geom_of(S, i);
-        int bx, by;
-        col_to_bxy(G, S.col[a][i], bx, by);
-        const int izi = S.iz[a][i];
-        const double xi = S.x[a][i], yi = S.y[a][i], zi = S.z[a][i];
-        const double ri = S.rad[i];
-        const float4 me = S.rel[a][i];
-        const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
-        // absolute slack bounding the FP32 distance error (offsets + bin widths)
-        const float slack = 8.0f * 1.1920929e-7f * fmaxf(dxb, fmaxf(dyb, dzb));
+    for (int base = blockIdx.x * blockDim.x; base < S.n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool act = i < S.n;
+        double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        walk<SORTED>(S, G, a, i, bx, by, izi, [&](const float4 q, auto slot, int dxs, int dys, int dzs, int sx, int sy) {
-            const float ex = (me.x - q.x) - (float)dxs * dxb;
-            const float ey = (me.y - q.y) - (float)dys * dyb;
-            const float ez = (me.z - q.z) - (float)dzs * dzb;
-            const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), bwf), slack);
-            if (r2f > __fmul_rn(lim, lim)) return;
-            const int j = slot();
-            const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
-            const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
-            const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            if (!G.nbh_trivial && !(r2 <= P.nbh)) return;  // not in the neighbour list
-            const double rj = S.rad[j];
-            const double rlm = ri + rj + P.bw;                // maxInteractionDistance
-            if (!(r2 <= (rlm - kSmall) * (rlm - kSmall))) return;
-            const double rS = ri + rj;
-            const double rA = rS + P.bw;
-            const double rn = sqrt(r2);
-            const double ux = dx / rn, uy = dy / rn, uz = dz / rn;
-            const double F = (rn < rA) ? -P.k * (rn - rA) * (rn - rA) * (rn - rS) : 0.0;
-            fx += F * ux;
-            fy += F * uy;
-            fz += F * uz;
-        });
-        // evaluateSurfaceForce, sphere branch: vcom = (0, 0, wall), vrot = 0
-        const double vx = fx + 0.0;
-        const double vy = fy + 0.0;
-        const double vz = fz + wall_law(zi, ri, P);
-        double nx = xi + dt * vx;
-        double ny = yi + dt * vy;
-        const double nz = zi + dt * vz;
-        if (G.per[0]) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
-        if (G.per[1]) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
-        S.x[b][i] = nx;
-        S.y[b][i] = ny;
-        S.z[b][i] = nz;
-        S.vx[i] = vx;
-        S.vy[i] = vy;
-        S.vz[i] = vz;
-        rebin_slot(S, G, i, nx, ny, nz, ri, b);
+        int col = 0, cnt = 0;
+        if (act) {
+            col = colony_of(S.cbase, S.ncol, i);
+            const DevGeom &G = S.geoms[col];
+            int bx, by;
+            col_to_bxy(G, S.col[a][i], bx, by);
+            const int izi = S.iz[a][i];
+            xi = S.x[a][i];
+            yi = S.y[a][i];
+            zi = S.z[a][i];
+            ri = S.rad[i];
+            const float4 me = S.rel[a][i];
+            const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
+            // absolute slack bounding the FP32 distance error (offsets + bin widths)
+            const float slack = 8.0f * 1.1920929e-7f * fmaxf(dxb, fmaxf(dyb, dzb));
+            int2 *mine = stage + lane * kStage64;
+            auto eval = [&](int j, int sx, int sy) {
+                double t[3];
+                if (sphere_term64(S, G, P, a, xi, yi, zi, ri, j, sx, sy, t)) {
+                    fx += t[0];
+                    fy += t[1];
+                    fz += t[2];
+                }
+            };
+            walk<SORTED>(S, G, a, i, bx, by, izi, [&](const float4 q, auto slot, int dxs, int dys, int dzs, int sx,
+                                                      int sy) {
+                const float ex = (me.x - q.x) - (float)dxs * dxb;
+                const float ey = (me.y - q.y) - (float)dys * dyb;
+                const float ez = (me.z - q.z) - (float)dzs * dzb;
+                const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+                const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), bwf), slack);
+                if (r2f > __fmul_rn(lim, lim)) return;
+                const int j = slot();
+                if (cnt < kStage64) {
+                    mine[cnt] = make_int2(j, (sx + 1) * 3 + (sy + 1));
+                } else {
+                    if (cnt == kStage64)  // too many for the stage: the staged ones first, in order
+                        for (int k = 0; k < kStage64; ++k) eval(mine[k].x, mine[k].y / 3 - 1, mine[k].y % 3 - 1);
+                    eval(j, sx, sy);
+                }
+                ++cnt;
+            });
+        }
+        // the warp's staged pairs, one per lane
+        const int xl = (cnt <= kStage64) ? cnt : 0;
+        int xo = xl;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, xo, d);
+            if (lane >= d) xo += v;
+        }
+        const int xt = __shfl_sync(0xffffffffu, xo, 31);
+        xo -= xl;
+        for (int t0 = 0; t0 < xt; t0 += 32) {
+            const int t = t0 + lane;
+            int o = 0;  // the slot that owns pair t: the last lane whose run starts at or before t
+            for (int s2 = 16; s2 >= 1; s2 >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, xo, o + s2);
+                if (v <= t) o += s2;
+            }
+            const double oxi = __shfl_sync(0xffffffffu, xi, o), oyi = __shfl_sync(0xffffffffu, yi, o);
+            const double ozi = __shfl_sync(0xffffffffu, zi, o), ori = __shfl_sync(0xffffffffu, ri, o);
+            const int oc = __shfl_sync(0xffffffffu, col, o);
+            const int oxo = __shfl_sync(0xffffffffu, xo, o);
+            bool pass = false;
+            double tt[3] = {0.0, 0.0, 0.0};
+            if (t < xt) {
+                const int2 e = stage[o * kStage64 + (t - oxo)];
+                pass = sphere_term64(S, S.geoms[oc], P, a, oxi, oyi, ozi, ori, e.x, e.y / 3 - 1, e.y % 3 - 1, tt);
+            }
+            const unsigned pm = __ballot_sync(0xffffffffu, pass);
+            term[lane] = tt[0];
+            term[32 + lane] = tt[1];
+            term[64 + lane] = tt[2];
+            __syncwarp();
+            const int k1 = min(xo + xl, t0 + 32);
+            for (int k = max(xo, t0); k < k1; ++k) {
+                if (!((pm >> (k - t0)) & 1u)) continue;
+                fx += term[k - t0];
+                fy += term[32 + k - t0];
+                fz += term[64 + k - t0];
+            }
+            __syncwarp();
+        }
+        if (act) {
+            const DevGeom &G = S.geoms[col];
+            // evaluateSurfaceForce, sphere branch: vcom = (0, 0, wall), vrot = 0
+            const double vx = fx + 0.0;
+            const double vy = fy + 0.0;
+            const double vz = fz + wall_law(zi, ri, P);
+            double nx = xi + dt * vx;
+            double ny = yi + dt * vy;
+            const double nz = zi + dt * vz;
+            if (G.per[0]) nx = wrap1(nx, G.plo[0], G.phi[0], G.len[0]);
+            if (G.per[1]) ny = wrap1(ny, G.plo[1], G.phi[1], G.len[1]);
+            S.x[b][i] = nx;
+            S.y[b][i] = ny;
+            S.z[b][i] = nz;
+            S.vx[i] = vx;
+            S.vy[i] = vy;
+            S.vz[i] = vz;
+            rebin_slot(S, G, i, nx, ny, nz, ri, b);
+        }
     }
 }
 
@@ -202,8 +303,10 @@ int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, 
 {
     const bool sorted = S.srel[a] != nullptr;  // the context keeps sorted copies; bare callers do not
     if (precision == BMXG_FP64_FORM) {
-        if (sorted) k_sphere64<true><<<grid, block, 0, st>>>(S, P, dt, a);
-        else k_sphere64<false><<<grid, block, 0, st>>>(S, P, dt, a);
+        // (block a multiple of 32: the warps stage and evaluate their pairs together)
+        const size_t smem = (size_t)(block / 32) * 32 * (kStage64 * sizeof(int2) + 3 * sizeof(double));
+        if (sorted) k_sphere64<true><<<grid, block, smem, st>>>(S, P, dt, a);
+        else k_sphere64<false><<<grid, block, smem, st>>>(S, P, dt, a);
     } else {
         if (sorted) k_sphere32<true><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
         else k_sphere32<false><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
