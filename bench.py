@@ -495,7 +495,9 @@ def run_ours(args):
 
     if args.eager and args.only_main:
         ctx.set_profiling(True)
-    # warm-up, then the timed K steps
+    # the step graphs instantiated up front (bmxg_prepare: no step runs), then
+    # the warm-up and the timed K steps
+    ctx.prepare(w.dt, prec)
     timed_steps(prec, max(args.warmup, 3))
     if world > 1:
         dist.barrier()
@@ -570,6 +572,7 @@ def run_ours(args):
     # the other form on the same workload, and the FP32F force error against FP64
     other = BMXG_FP64 if prec == BMXG_FP32F else BMXG_FP32F
     ctx.set_state(w.particles, w.offsets)
+    ctx.prepare(w.dt, other)
     timed_steps(other, 3)
     ms_other = timed_steps(other, args.steps)
     v_other = N * args.steps / (ms_other / 1e3)

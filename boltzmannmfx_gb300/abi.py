@@ -80,6 +80,11 @@ class Stats(C.Structure):
                 ("main_kernel_ms", C.c_double), ("last_step_ms", C.c_double)]
 
 
+class Tile(C.Structure):
+    """bmxg_tile: first and last cell per axis (0-based, inclusive)."""
+    _fields_ = [("lo", C.c_int32 * 3), ("hi", C.c_int32 * 3)]
+
+
 class Shapes(C.Structure):
     """bmxg_shapes: the launch shapes in use."""
     _fields_ = [("sphere_block", C.c_int32 * 2), ("sphere_grid", C.c_int32 * 2),

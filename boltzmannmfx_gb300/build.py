@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbmxg.so")
-SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "k_adjoint.cu", "k_noalloc.cu", "k_list.cu", "k_split.cu",
+SOURCES = ["k_bin.cu", "k_sphere.cu", "k_rod.cu", "k_adjoint.cu", "k_noalloc.cu", "k_list.cu", "k_split.cu", "k_tile.cu",
            "bmxg_ctx.cu", "bmxg_aos.cpp", "bmxg_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -11,6 +11,7 @@
 #include <functional>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -1150,25 +1151,11 @@ int get_graph(bmxg_ctx *ctx, double dt, int precision, int parity, cudaGraphExec
     return BMXG_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
+// What a call of nsteps steps in this form needs before it enqueues them:
+// the list or exact bins, the buffers of the path it takes (graphs captured
+// before an allocation are dropped: they hold the state's pointers by value).
+int step_setup(bmxg_ctx *ctx, int32_t nsteps, int32_t precision)
 {
-    if (!ctx) return BMXG_ERR_ARG;
-    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
-    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
-    if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt or nsteps");
-    if (precision != BMXG_FP64 && precision != BMXG_FP32F) return fail(ctx, BMXG_ERR_ARG, "bad precision");
-    if (ctx->n == 0 || nsteps == 0) return BMXG_OK;
-    // nsubsteps = ceil(dt / dtsolid) with dtsolid := dt, subdt = dt / nsubsteps
-    // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
-    const double subdt = dt / 1.0;
-    // FP32F spheres use the neighbour list wherever it reproduces the pair set,
-    // and where the steps are many enough to amortise a build: the first call
-    // after a load, if shorter than kListMinSteps, takes the per-step path (a
-    // load-step-store caller never reuses a list); later calls build one
     float skin = (precision == BMXG_FP32F && ctx->list_mode) ? list_skin(ctx) : 0.0f;
     if (skin > 0.0f && !ctx->list_valid && nsteps < kListMinSteps && ctx->step_count == 0) skin = 0.0f;
     if (skin > 0.0f) {
@@ -1205,6 +1192,50 @@ int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
         ctx->S.rctl = ctl;
         drop_graphs(ctx);
     }
+    return BMXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmxg_prepare(bmxg_ctx *ctx, double dt, int32_t precision)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (!std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt");
+    if (precision != BMXG_FP64 && precision != BMXG_FP32F) return fail(ctx, BMXG_ERR_ARG, "bad precision");
+    if (ctx->n == 0 || ctx->profiling) return BMXG_OK;
+    const double subdt = dt / 1.0;
+    if (int rc = step_setup(ctx, 2 * kResyncEvery, precision)) return rc;
+    // the replayed graph of kResyncEvery steps and the one-step graphs (with and
+    // without the re-sync), from either parity
+    for (int parity = 0; parity < 2; ++parity) {
+        cudaGraphExec_t g = nullptr;
+        if (int rc = get_graph(ctx, subdt, precision, parity, &g)) return rc;
+        for (int resync = 0; resync < 2; ++resync)
+            if (int rc = get_graph(ctx, subdt, precision, parity, &g, resync)) return rc;
+    }
+    return BMXG_OK;
+}
+
+int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
+    if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
+    if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt or nsteps");
+    if (precision != BMXG_FP64 && precision != BMXG_FP32F) return fail(ctx, BMXG_ERR_ARG, "bad precision");
+    if (ctx->n == 0 || nsteps == 0) return BMXG_OK;
+    // nsubsteps = ceil(dt / dtsolid) with dtsolid := dt, subdt = dt / nsubsteps
+    // (bmx_pc_interaction.cpp:56-65): one substep of dt / 1
+    const double subdt = dt / 1.0;
+    // FP32F spheres use the neighbour list wherever it reproduces the pair set,
+    // and where the steps are many enough to amortise a build: the first call
+    // after a load, if shorter than kListMinSteps, takes the per-step path (a
+    // load-step-store caller never reuses a list); later calls build one
+    if (int rc = step_setup(ctx, nsteps, precision)) return rc;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int32_t left = nsteps;
     ctx->kev_used = 0;
@@ -1320,6 +1351,121 @@ int bmxg_set_profiling(bmxg_ctx *ctx, int32_t on)
         ctx->stats.main_kernel_ms = 0.0;
         ctx->stats.main_kernel_launches = 0;
     }
+    return BMXG_OK;
+}
+
+int bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *reals, const bmxg_particles *ghosts,
+                   double dt, int32_t where)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
+    if (!tile || !reals || reals->n < 0 || (ghosts && ghosts->n < 0)) return fail(ctx, BMXG_ERR_ARG, "bad arguments");
+    if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
+    if (!std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt");
+    if (ctx->ncol != 1)
+        return fail(ctx, BMXG_ERR_UNSUPPORTED, "a tile step takes a context of one geometry (the level's domain)");
+    const int64_t nr = reals->n, ng = ghosts ? ghosts->n : 0;
+    if (nr == 0) return BMXG_OK;
+    if (!reals->x || !reals->y || !reals->z || !reals->radius || !reals->cell_type || !reals->velx || !reals->vely ||
+        !reals->velz)
+        return fail(ctx, BMXG_ERR_ARG, "reals need x, y, z, radius, cell_type and velx, vely, velz");
+    if (ng && (!ghosts->x || !ghosts->y || !ghosts->z || !ghosts->radius || !ghosts->cell_type))
+        return fail(ctx, BMXG_ERR_ARG, "ghosts need x, y, z, radius and cell_type");
+    if (nr + ng >= (1LL << 30)) return fail(ctx, BMXG_ERR_UNSUPPORTED, "more than 2^30 particles in a tile");
+    const bmxg_geometry &g = ctx->geoms[0];
+    TileGeom T;
+    std::memset(&T, 0, sizeof(T));
+    double diag2 = 0.0;
+    int64_t ncells = 1;
+    for (int d = 0; d < 3; ++d) {
+        T.plo[d] = g.prob_lo[d];
+        T.phi[d] = g.prob_hi[d];
+        T.len[d] = g.prob_hi[d] - g.prob_lo[d];
+        T.n[d] = g.n_cell[d];
+        const double dx = T.len[d] / (double)T.n[d];  // the whole-domain step's bin width and inverse
+        T.dxi[d] = 1.0 / dx;
+        T.per[d] = g.is_periodic[d] ? 1 : 0;
+        if (tile->lo[d] < 0 || tile->hi[d] < tile->lo[d] || tile->hi[d] >= T.n[d])
+            return fail(ctx, BMXG_ERR_ARG, "the tile is not a box of the domain's cells");
+        T.lo[d] = tile->lo[d];
+        T.nt[d] = tile->hi[d] - tile->lo[d] + 1;
+        ncells *= T.nt[d] + 2;
+        diag2 += 4.0 * dx * dx;
+    }
+    if (ncells >= (1LL << 30)) return fail(ctx, BMXG_ERR_UNSUPPORTED, "a tile of more than 2^30 cells");
+    T.nbh_trivial = (ctx->prm.neighborhood >= diag2 * (1.0 + 1e-9)) ? 1 : 0;
+    const int64_t nt = nr + ng;
+    cudaStream_t st = ctx->stream;
+    // stream-ordered scratch for the call
+    std::vector<void *> mem;
+    auto alloc = [&](auto **p, size_t count) -> bool {
+        void *q = nullptr;
+        if (cudaMallocAsync(&q, std::max<size_t>(count, 1) * sizeof(**p), st) != cudaSuccess) return false;
+        mem.push_back(q);
+        *p = reinterpret_cast<std::remove_reference_t<decltype(*p)>>(q);
+        return true;
+    };
+    auto release = [&]() {
+        for (void *q : mem) cudaFreeAsync(q, st);
+        mem.clear();
+    };
+    TileBufs B;
+    int *scratch = nullptr;
+    const bool ok = alloc(&B.x, nt) && alloc(&B.y, nt) && alloc(&B.z, nt) && alloc(&B.r, nt) && alloc(&B.ct, nt) &&
+                    alloc(&B.ox, nr) && alloc(&B.oy, nr) && alloc(&B.oz, nr) && alloc(&B.vx, nr) &&
+                    alloc(&B.vy, nr) && alloc(&B.vz, nr) && alloc(&B.cell, nt) && alloc(&B.cnt, ncells) &&
+                    alloc(&B.start, ncells + 1) && alloc(&B.fill, ncells) && alloc(&B.perm, nt) &&
+                    alloc(&B.bad, 2) && alloc(&scratch, scan_scratch_ints((int)ncells));
+    if (!ok) {
+        release();
+        (void)cudaGetLastError();
+        return fail(ctx, BMXG_ERR_OOM, "tile scratch");
+    }
+    const cudaMemcpyKind kin = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    const cudaMemcpyKind kout = (where == BMXG_HOST) ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaSuccess;
+    auto in = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, kin, st);
+    };
+    in(B.x, reals->x, 8 * nr);
+    in(B.y, reals->y, 8 * nr);
+    in(B.z, reals->z, 8 * nr);
+    in(B.r, reals->radius, 8 * nr);
+    in(B.ct, reals->cell_type, 4 * nr);
+    if (ng) {
+        in(B.x + nr, ghosts->x, 8 * ng);
+        in(B.y + nr, ghosts->y, 8 * ng);
+        in(B.z + nr, ghosts->z, 8 * ng);
+        in(B.r + nr, ghosts->radius, 8 * ng);
+        in(B.ct + nr, ghosts->cell_type, 4 * ng);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.cnt, 0, sizeof(int) * ncells, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.fill, 0, sizeof(int) * ncells, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.bad, 0, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) {
+        ctx->launches += launch_tile_step(B, T, dev_params(ctx->prm), dt / 1.0, (int)nr, (int)nt, scratch, ctx->nsm, st);
+        e = cudaGetLastError();
+    }
+    unsigned long long bad[2] = {0ull, 0ull};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(bad, B.bad, sizeof(bad), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && !bad[0] && !bad[1]) {
+        auto out = [&](void *dst, const void *src) {
+            if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, 8 * nr, kout, st);
+        };
+        out(reals->x, B.ox);
+        out(reals->y, B.oy);
+        out(reals->z, B.oz);
+        out(reals->velx, B.vx);
+        out(reals->vely, B.vy);
+        out(reals->velz, B.vz);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    release();
+    if (e != cudaSuccess) return fail(ctx, BMXG_ERR_CUDA, std::string("tile step: ") + cudaGetErrorString(e));
+    if (bad[1]) return fail(ctx, BMXG_ERR_UNSUPPORTED, "the tile step takes spheres (YEAST) only");
+    if (bad[0])
+        return fail(ctx, BMXG_ERR_ARG, "a real particle outside the tile or a ghost outside its one-cell halo");
     return BMXG_OK;
 }
 

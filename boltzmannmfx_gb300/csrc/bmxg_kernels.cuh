@@ -213,6 +213,29 @@ constexpr int kListBodyKernels = 12;
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
                      cudaStream_t st);
 
+// ---- one tile with the caller's ghosts (k_tile.cu) -------------------------
+// The level's domain and the tile: cells are the domain's (1-based bins of
+// the whole-domain step) offset by lo, the tile's first cell minus one, so
+// that the tile's own cells are 1..nt and the one-cell halo 0 and nt + 1.
+struct TileGeom {
+    double plo[3], phi[3], len[3], dxi[3];
+    int n[3], per[3];
+    int lo[3], nt[3];
+    int nbh_trivial;
+};
+// Device buffers of one tile call: positions, radii and cell types of the
+// reals then the ghosts; the reals' outputs; cell scratch and counters.
+struct TileBufs {
+    double *x, *y, *z, *r;
+    int *ct;
+    double *ox, *oy, *oz, *vx, *vy, *vz;
+    int *cell, *cnt, *start, *fill, *perm;
+    unsigned long long *bad;  // [2]: a real outside the tile or a ghost outside the halo; a non-sphere
+};
+// bin, count, scan, scatter, order each cell by index, step the reals
+int launch_tile_step(const TileBufs &B, const TileGeom &T, const DevParams &P, double dt, int nreal, int ntot,
+                     int *scan_scratch, int nsm, cudaStream_t st);
+
 // ---- rods and mixed states (k_rod.cu) ------------------------------------
 int launch_rod_mobility(const DevState &S, const DevParams &P, int grid, int block, cudaStream_t st);
 // list: also record each segment's gated pairs (the FP32F pipeline)

@@ -27,7 +27,7 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
                "bmxg_particle_exchange", "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk",
                "bmxg_read_checkpoint",
-               "bmxg_io_last_error", "bmxg_autotune", "bmxg_get_shapes", "bmxg_split_cells_aos", "bmxg_set_pair_capture",
+               "bmxg_io_last_error", "bmxg_autotune", "bmxg_get_shapes", "bmxg_step_tile", "bmxg_prepare", "bmxg_split_cells_aos", "bmxg_set_pair_capture",
                "bmxg_get_step_pairs")
 
 
@@ -63,6 +63,9 @@ def load_library(path=None):
     L.bmxg_set_state.argtypes = [vp, C.POINTER(ParticlesStruct), C.POINTER(C.c_int64), C.c_int]
     L.bmxg_get_state.argtypes = [vp, C.POINTER(ParticlesStruct), C.c_int]
     L.bmxg_step.argtypes = [vp, C.c_double, C.c_int32, C.c_int32]
+    L.bmxg_prepare.argtypes = [vp, C.c_double, C.c_int32]
+    L.bmxg_step_tile.argtypes = [vp, C.POINTER(abi.Tile), C.POINTER(ParticlesStruct), C.POINTER(ParticlesStruct),
+                                 C.c_double, C.c_int32]
     L.bmxg_evolve_particles.argtypes = [vp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     L.bmxg_evolve_particles_aos.argtypes = [vp, vp, C.c_int64, C.c_int32, C.c_int32,
                                             C.POINTER(C.c_int64), C.c_double, C.POINTER(C.c_double),
@@ -159,6 +162,23 @@ class Context:
 
     def step(self, dt, nsteps=1, precision=abi.BMXG_FP64):
         self._check(self.lib.bmxg_step(self.h, dt, nsteps, precision))
+
+    def prepare(self, dt, precision=abi.BMXG_FP64):
+        """Instantiate the step graphs of (dt, precision) without stepping (bmxg_prepare)."""
+        self._check(self.lib.bmxg_prepare(self.h, dt, precision))
+
+    def step_tile(self, lo, hi, reals, ghosts, dt):
+        """One FP64 step of the spheres of tile [lo, hi] (cells, inclusive) with
+        the caller's ghosts (bmxg_step_tile): reals' x, y, z and velx, vely,
+        velz are written in place."""
+        t = abi.Tile()
+        t.lo[:] = [int(v) for v in lo]
+        t.hi[:] = [int(v) for v in hi]
+        sr = reals.struct(("x", "y", "z", "radius", "cell_type", "velx", "vely", "velz"))
+        sg = ghosts.struct(("x", "y", "z", "radius", "cell_type")) if ghosts is not None and ghosts.n else None
+        self._check(self.lib.bmxg_step_tile(self.h, C.byref(t), C.byref(sr), C.byref(sg) if sg else None, dt,
+                                            abi.BMXG_HOST))
+        return reals
 
     def evolve_particles(self, dt):
         cost = (C.c_double * len(self.geoms))()

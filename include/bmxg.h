@@ -185,6 +185,14 @@ int  bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where);
  * replayed from a captured CUDA graph. */
 int  bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision);
 
+/* Instantiate, without running a step, the CUDA graphs that bmxg_step(ctx, dt,
+ * n, precision) replays (the graph of the re-sync period and the one-step
+ * graphs, from either parity) and allocate the buffers of that path, so that
+ * the first long call captures nothing.  The FP32F list path counts as chosen
+ * (a later one-step call then steps over the list too).  No counterpart in the
+ * reference (it has no graphs). */
+int  bmxg_prepare(bmxg_ctx *ctx, double dt, int32_t precision);
+
 /* Drop-in for the reference member function, on the state loaded with
  * bmxg_set_state: nsubsteps is written (always 1), cost_per_colony (may be
  * NULL) receives the particle count per colony as the "NumParticles" cost
@@ -449,6 +457,35 @@ int  bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode);
  * as it was.  The reference has no counterpart (AMReX tiles its loops by a
  * fixed tile size, bmx_pc_interaction.cpp:111-114). */
 int  bmxg_autotune(bmxg_ctx *ctx, const char *cache_path);
+
+/* ---- one tile with the caller's ghost particles ------------------------- */
+
+/* A tile of the level's domain (the context's one geometry): its first and
+ * last cell per axis, 0-based and inclusive (an AMReX Box). */
+typedef struct bmxg_tile {
+    int32_t lo[3];
+    int32_t hi[3];
+} bmxg_tile;
+
+/* One FP64 step of the spheres (YEAST) of one tile: AMReX's per-tile
+ * EvolveParticles (src/des/bmx_pc_interaction.cpp:97-279) after fillNeighbors
+ * has put the particles within one cell of the tile beside its own -- the
+ * ghosts, periodic images already shifted by a domain length (the halo of
+ * src/des/bmx_pc.cpp:23).  reals: x, y, z, radius, cell_type in; x, y, z
+ * replaced by the new positions (periodically wrapped, as the trailing
+ * Redistribute does) and velx, vely, velz written.  ghosts (NULL or n = 0:
+ * none): x, y, z, radius, cell_type, read only.  The neighbour list holds the
+ * reals and the ghosts in the order of the whole-domain step (cells x, y, z;
+ * within a cell the reals in the caller's order, then the ghosts in theirs),
+ * so that tiles covering the domain, each with the ghosts the whole-domain
+ * step would see, give the whole-domain step's results bit for bit.  The
+ * context needs no loaded state; its one geometry is the level's domain.
+ * where: BMXG_HOST or BMXG_DEVICE for every array.  Returns BMXG_ERR_ARG when
+ * a real particle is outside the tile or a ghost outside its one-cell halo,
+ * BMXG_ERR_UNSUPPORTED for a particle that is not YEAST (rod segments need
+ * their neighbours' bond tables: a whole-domain step). */
+int  bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *reals,
+                    const bmxg_particles *ghosts, double dt, int32_t where);
 
 /* The launch shapes in use (defaults until bmxg_autotune picks others). */
 typedef struct bmxg_shapes {

@@ -254,3 +254,27 @@ def test_autotune_list_shapes_leave_state_and_steps_unchanged(gpu_lib, tmp_path)
     assert C.shapes() == sh
     for c in (A, B, C):
         c.close()
+
+
+def test_prepare_instantiates_graphs_and_changes_no_result(gpu_lib):
+    """bmxg_prepare captures the step graphs without stepping: the state is
+    unchanged, and the steps after it are bit-identical to those of a context
+    that captured them on first use (FP32F list path and FP64)."""
+    w = configs.sphere_fp32(n=20_000)
+    A, B = ctx_for(w), ctx_for(w)
+    A.prepare(w.dt, BMXG_FP32F)
+    Q0 = read(A, w.particles)
+    for k in ("x", "y", "z"):
+        assert np.array_equal(Q0[k], w.particles[k]), k
+    for prec in (BMXG_FP32F, BMXG_FP64):
+        if prec == BMXG_FP64:
+            for c in (A, B):
+                c.set_state(w.particles, w.offsets)
+            A.prepare(w.dt, prec)
+        A.step(w.dt, 20, prec)
+        B.step(w.dt, 20, prec)
+        QA, QB = read(A, w.particles), read(B, w.particles)
+        for k in ("x", "y", "z", "velx", "vely", "velz"):
+            assert np.array_equal(QA[k], QB[k]), (prec, k)
+    A.close()
+    B.close()
