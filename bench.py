@@ -549,6 +549,8 @@ def run_ours(args):
     achieved = alg / (k_ms / 1e3) / 1e9
     if list_mode:
         kname = "k_list_step"
+    elif kind == "rod" and prec == BMXG_FP32F:  # the events bracket the three kernels of the rod pipeline
+        kname = "k_rod_pair32 + k_rod_pair64 + k_rod_seg32"
     else:
         kname = ("k_sphere" if kind == "sphere" else "k_rod_force") + ("<FP32F>" if prec == BMXG_FP32F else "<FP64>")
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
