@@ -349,7 +349,8 @@ def sample_colonies(w, target):
         return w.particles, list(w.geoms), np.asarray(w.offsets), ncol
     order = np.argsort(sizes, kind="stable")
     k = max(1, int(round(sizes.sum() / max(target, 1))))
-    pick = np.sort(order[k // 2::k])
+    # (at least one colony: a colony is the smallest unit the step runs on)
+    pick = np.sort(order[min(k // 2, ncol - 1)::k])
     parts = [w.particles.subset(int(w.offsets[c]), int(w.offsets[c + 1])) for c in pick]
     P = Particles.concat(parts)
     off = np.zeros(len(pick) + 1, np.int64)

@@ -58,3 +58,20 @@ def test_rod_trees_topology():
             dv[0] -= round(dv[0] / 0.512) * 0.512
             dv[1] -= round(dv[1] / 0.512) * 0.512
             assert np.linalg.norm(dv) < 1e-12
+
+
+def test_bench_cpu_samples_keep_whole_colonies():
+    """The CPU arm's stratified sample: whole colonies in the workload's size
+    mix, at least one even when a single colony exceeds the target."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    w = configs.sphere_fp32()
+    P, g, off, take = bench.sample_colonies(w, 50_000)
+    assert take == 1 and P.n == w.n and list(off) == [0, w.n]
+    w = configs.colonies(ncol=24)
+    P, g, off, take = bench.sample_colonies(w, w.n // 4)
+    assert 1 <= take < 24 and P.n == off[-1] and len(g) == take
+    sizes = np.diff(w.offsets)
+    assert set(np.diff(off).tolist()) <= set(sizes.tolist())
