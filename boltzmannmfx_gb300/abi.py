@@ -89,7 +89,7 @@ class Shapes(C.Structure):
     """bmxg_shapes: the launch shapes in use."""
     _fields_ = [("sphere_block", C.c_int32 * 2), ("sphere_grid", C.c_int32 * 2),
                 ("list_step_block", C.c_int32), ("list_step_passes", C.c_int32),
-                ("list_build_block", C.c_int32), ("reserved", C.c_int32)]
+                ("list_build_block", C.c_int32), ("list_step_persistent", C.c_int32)]
 
 
 class SplitParams(C.Structure):

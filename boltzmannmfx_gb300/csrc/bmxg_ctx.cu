@@ -81,6 +81,7 @@ struct bmxg_ctx {
     // list path shapes (bmxg_autotune): k_list_step's block and passes per
     // chunk (0: the launcher's rule), k_list_build's block
     int ls_block = kListStepBlock, ls_passes = 0, lb_block = kListBuildBlock;
+    bool ls_persist = false;  // the list step as one wave of blocks taking chunks from a counter
     bmxg_stats stats{};
     int64_t launches = 0;                   // kernels enqueued (graph nodes counted per replay)
     bool profiling = false;
@@ -1068,7 +1069,7 @@ int enqueue_list_step(bmxg_ctx *ctx, double dt, int a)
     cudaEvent_t k0, k1;
     prof_events(ctx, &k0, &k1);
     if (k0) cudaEventRecord(k0, st);
-    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, ctx->ls_block, ctx->ls_passes, st));
+    LAUNCH(launch_list_step(S, P, dt, a, ctx->nsm, ctx->ls_block, ctx->ls_passes, st, ctx->ls_persist));
     if (k1) cudaEventRecord(k1, st);
     return BMXG_OK;
 }
@@ -1773,13 +1774,15 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
                       hist.c_str());
         const std::string txt = cache_read();
         const size_t pos = txt.find(key);
-        int sb = 0, sp = 0, bb = 0;
+        int sb = 0, sp = 0, bb = 0, pe = 0;
         if (pos != std::string::npos &&
             std::sscanf(txt.c_str() + pos + std::strlen(key),
-                        ": {\"step_block\": %d, \"step_passes\": %d, \"build_block\": %d", &sb, &sp, &bb) == 3 &&
+                        ": {\"step_block\": %d, \"step_passes\": %d, \"step_persistent\": %d, \"build_block\": %d",
+                        &sb, &sp, &pe, &bb) == 4 &&
             sb > 0 && bb > 0) {
             ctx->ls_block = sb;
             ctx->ls_passes = sp;
+            ctx->ls_persist = pe != 0;
             ctx->lb_block = bb;
         } else {
             // a list built on the loaded positions; then the step launches read
@@ -1794,16 +1797,23 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
             ctx->launches += launch_list_rebuild(S, P, a, ctx->cell_scratch, mgrd, mblk, ctx->lb_block, st);
             float best = 1e30f, best_b = 1e30f;
             int best_sb = ctx->ls_block, best_sp = ctx->ls_passes, best_bb = ctx->lb_block;
+            bool best_pe = ctx->ls_persist;
             for (int blk : {64, 128, 256}) {
-                for (int passes : {1, 2, 4}) {
-                    float ms = 0.0f;
-                    if (int rc = timeit(2, 5, [&]() { return launch_list_step(S, P, 0.0, a, ctx->nsm, blk, passes,
-                                                                                st); }, &ms))
-                        return rc;
-                    if (ms < best) {
-                        best = ms;
-                        best_sb = blk;
-                        best_sp = passes;
+                // one block per chunk of 1, 2 or 4 passes; or one persistent wave
+                // taking chunks of 2, 4 or 8 passes from the dispenser
+                for (int pe = 0; pe < 2; ++pe) {
+                    for (int passes : {1, 2, 4}) {
+                        const int pp = pe ? 2 * passes : passes;
+                        float ms = 0.0f;
+                        if (int rc = timeit(2, 5, [&]() { return launch_list_step(S, P, 0.0, a, ctx->nsm, blk, pp,
+                                                                                    st, pe != 0); }, &ms))
+                            return rc;
+                        if (ms < best) {
+                            best = ms;
+                            best_sb = blk;
+                            best_sp = pp;
+                            best_pe = pe != 0;
+                        }
                     }
                 }
                 float ms = 0.0f;
@@ -1817,15 +1827,39 @@ int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
             CK(cudaStreamSynchronize(st));
             ctx->ls_block = best_sb;
             ctx->ls_passes = best_sp;
+            ctx->ls_persist = best_pe;
             ctx->lb_block = best_bb;
             ctx->list_valid = false;
             std::snprintf(entry, sizeof(entry),
-                          "%s: {\"step_block\": %d, \"step_passes\": %d, \"build_block\": %d, \"step_ms_per_5\": "
-                          "%.4f, \"build_ms_per_3\": %.4f}",
-                          key, best_sb, best_sp, best_bb, best, best_b);
+                          "%s: {\"step_block\": %d, \"step_passes\": %d, \"step_persistent\": %d, \"build_block\": "
+                          "%d, \"step_ms_per_5\": %.4f, \"build_ms_per_3\": %.4f}",
+                          key, best_sb, best_sp, best_pe ? 1 : 0, best_bb, best, best_b);
             cache_add(entry);
         }
     }
+    drop_graphs(ctx);
+    return BMXG_OK;
+}
+
+int bmxg_set_shapes(bmxg_ctx *ctx, const bmxg_shapes *in)
+{
+    if (!ctx) return BMXG_ERR_ARG;
+    if (!in) return fail(ctx, BMXG_ERR_ARG, "no shapes");
+    auto block_ok = [](int b) { return b >= 32 && b <= 256 && b % 32 == 0; };
+    for (int k = 0; k < 2; ++k)
+        if (!block_ok(in->sphere_block[k]) || in->sphere_grid[k] < 0)
+            return fail(ctx, BMXG_ERR_ARG, "sphere block: a multiple of 32 up to 256; grid >= 0");
+    if (!block_ok(in->list_step_block) || !block_ok(in->list_build_block) || in->list_step_passes < 0 ||
+        in->list_step_passes > 64)
+        return fail(ctx, BMXG_ERR_ARG, "list blocks: a multiple of 32 up to 256; passes 0..64");
+    for (int k = 0; k < 2; ++k) {
+        ctx->sh_sphere[k].block = in->sphere_block[k];
+        ctx->sh_sphere[k].grid = in->sphere_grid[k];
+    }
+    ctx->ls_block = in->list_step_block;
+    ctx->ls_passes = in->list_step_passes;
+    ctx->ls_persist = in->list_step_persistent != 0;
+    ctx->lb_block = in->list_build_block;
     drop_graphs(ctx);
     return BMXG_OK;
 }
@@ -1841,6 +1875,7 @@ int bmxg_get_shapes(const bmxg_ctx *ctx, bmxg_shapes *out)
     out->list_step_block = ctx->ls_block;
     out->list_step_passes = ctx->ls_passes;
     out->list_build_block = ctx->lb_block;
+    out->list_step_persistent = ctx->ls_persist ? 1 : 0;
     return BMXG_OK;
 }
 

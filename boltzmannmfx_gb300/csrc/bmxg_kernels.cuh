@@ -38,6 +38,9 @@ struct ListCtl {
     int builds;            // builds decided so far
     unsigned long long body_runs;  // builds actually run (counted by the first build kernel)
     unsigned long long overflow;   // slots whose list exceeded the capacity (last build)
+    // the persistent list step's chunk dispenser: the next chunk to hand out
+    // and the blocks that found none left; the last of them resets both
+    unsigned next_chunk, done_blocks;
 };
 
 constexpr int kNbrCap = 32;          // list entries per slot (more: the slot walks its stencil)
@@ -209,9 +212,11 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
 int launch_list_build(const DevState &S, const DevParams &P, int build_block, cudaStream_t st);
 constexpr int kListBodyKernels = 12;
 // force + wall + update over the list, reading buffer a and writing buffer b
-// (grid = the SM count; passes of the block per chunk of slots, <= 0: a rule)
+// (grid = the SM count; passes of the block per chunk of slots, <= 0: a rule;
+// persistent: one wave of blocks taking chunks from a counter, else one block
+// per chunk)
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
-                     cudaStream_t st);
+                     cudaStream_t st, bool persistent = false);
 
 // ---- one tile with the caller's ghosts (k_tile.cu) -------------------------
 // The level's domain and the tile: cells are the domain's (1-based bins of

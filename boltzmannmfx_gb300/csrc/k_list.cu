@@ -395,7 +395,7 @@ __global__ void k_list_xcopy(const DevState S)
 // a dozen) from the compacted list, where a warp's entries lie together: a
 // few sectors per warp, not one per entry as a plane per list position would
 // cost.
-template <bool CAP>
+template <bool CAP, bool PERSIST>
 __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const DevParams P, float dtf, int a, int chunk)
 {
     constexpr int B = kListBins;
@@ -415,7 +415,18 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
         wmax[w][lane] = kKeyNegInf;
     }
     __syncwarp();
-    const int i0 = blockIdx.x * chunk;
+    // the chunks of consecutive slots this block takes: its own, or (persistent)
+    // the next from the dispenser until none is left
+    __shared__ int s_chunk;
+    const int nchunks = (n + chunk - 1) / chunk;
+    int ck = blockIdx.x;
+    if (PERSIST) {
+        if (threadIdx.x == 0) s_chunk = (int)atomicAdd(&S.lctl->next_chunk, 1u);
+        __syncthreads();
+        ck = s_chunk;
+    }
+    while (ck < nchunks) {
+    const int i0 = ck * chunk;
     const int i1 = min(i0 + chunk, n);
     int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.cbase, S.ncol, i0 + threadIdx.x) : 0;
     for (int base = i0; base < i1; base += blockDim.x) {  // same trip count for every thread
@@ -563,6 +574,21 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
             wmax[w][1] = max(wmax[w][1], hi1);
             wmin[w][2] = min(wmin[w][2], lo2);
             wmax[w][2] = max(wmax[w][2], hi2);
+        }
+    }
+    if (!PERSIST) break;
+    __syncthreads();  // every thread has read s_chunk
+    if (threadIdx.x == 0) s_chunk = (int)atomicAdd(&S.lctl->next_chunk, 1u);
+    __syncthreads();
+    ck = s_chunk;
+    }
+    if (PERSIST && threadIdx.x == 0) {
+        // the last block to find the dispenser empty resets it for the next launch
+        __threadfence();
+        if (atomicAdd(&S.lctl->done_blocks, 1u) == gridDim.x - 1) {
+            S.lctl->next_chunk = 0u;
+            S.lctl->done_blocks = 0u;
+            __threadfence();
         }
     }
     // then over the block: six atomics per block, not per warp (updates of
@@ -751,7 +777,7 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
 }
 
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
-                     cudaStream_t st)
+                     cudaStream_t st, bool persistent)
 {
     // passes of the block per chunk (passes <= 0: the rule): short enough that
     // the block scheduler evens out the uneven list lengths of the colonies
@@ -765,8 +791,15 @@ int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, in
         chunk = (two >= 4 * (1536 / block) * grid) ? 2 * block : block;
     }
     const int nb = (S.n + chunk - 1) / chunk;
-    if (S.pcap) k_list_step<true><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
-    else k_list_step<false><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
+    if (persistent) {
+        // one wave: the blocks that fit on the SMs at once (1536 threads per SM)
+        const int wave = std::max(1, std::min(nb, grid * (1536 / block)));
+        if (S.pcap) k_list_step<true, true><<<wave, block, 0, st>>>(S, P, (float)dt, a, chunk);
+        else k_list_step<false, true><<<wave, block, 0, st>>>(S, P, (float)dt, a, chunk);
+    } else {
+        if (S.pcap) k_list_step<true, false><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
+        else k_list_step<false, false><<<nb, block, 0, st>>>(S, P, (float)dt, a, chunk);
+    }
     return 1;
 }
 

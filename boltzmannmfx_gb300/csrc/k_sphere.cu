@@ -87,7 +87,7 @@ __device__ __forceinline__ bool sphere_term64(const DevState &S, const DevGeom &
 // the same order as a walk that evaluates each pair when it meets it, so the
 // result stays bit-identical to the oracle.  A slot with more than kStage64
 // staged candidates evaluates them itself, in order, as it walks.
-constexpr int kStage64 = 8;
+constexpr int kStage64 = 16;
 
 template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)

@@ -27,7 +27,7 @@ ABI_SYMBOLS = ("bmxg_version", "bmxg_last_error", "bmxg_create", "bmxg_destroy",
                "bmxg_backward", "bmxg_sphere_step_noalloc", "bmxg_init_bonds", "bmxg_set_list_mode",
                "bmxg_particle_exchange", "bmxg_read_ascii", "bmxg_write_ascii", "bmxg_write_vtk",
                "bmxg_read_checkpoint",
-               "bmxg_io_last_error", "bmxg_autotune", "bmxg_get_shapes", "bmxg_step_tile", "bmxg_prepare", "bmxg_split_cells_aos", "bmxg_set_pair_capture",
+               "bmxg_io_last_error", "bmxg_autotune", "bmxg_get_shapes", "bmxg_step_tile", "bmxg_prepare", "bmxg_set_shapes", "bmxg_split_cells_aos", "bmxg_set_pair_capture",
                "bmxg_get_step_pairs")
 
 
@@ -76,6 +76,7 @@ def load_library(path=None):
                                  C.c_int64, C.POINTER(C.c_int64)]
     L.bmxg_autotune.argtypes = [vp, C.c_char_p]
     L.bmxg_get_shapes.argtypes = [vp, C.POINTER(abi.Shapes)]
+    L.bmxg_set_shapes.argtypes = [vp, C.POINTER(abi.Shapes)]
     L.bmxg_init_bonds.argtypes = [vp, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.bmxg_set_list_mode.argtypes = [vp, C.c_int32]
     L.bmxg_set_pair_capture.argtypes = [vp, C.c_int32]
@@ -287,13 +288,26 @@ class Context:
     def autotune(self, cache_path=None):
         self._check(self.lib.bmxg_autotune(self.h, cache_path.encode() if cache_path else None))
 
+    def set_shapes(self, **kw):
+        """Pin launch shapes (bmxg_set_shapes): the current ones with the given keys replaced."""
+        cur = self.shapes()
+        cur.update(kw)
+        sh = abi.Shapes()
+        sh.sphere_block[:] = cur["sphere_block"]
+        sh.sphere_grid[:] = cur["sphere_grid"]
+        sh.list_step_block = cur["list_step_block"]
+        sh.list_step_passes = cur["list_step_passes"]
+        sh.list_build_block = cur["list_build_block"]
+        sh.list_step_persistent = 1 if cur["list_step_persistent"] else 0
+        self._check(self.lib.bmxg_set_shapes(self.h, C.byref(sh)))
+
     def shapes(self):
         """The launch shapes in use (bmxg_get_shapes)."""
         sh = abi.Shapes()
         self._check(self.lib.bmxg_get_shapes(self.h, C.byref(sh)))
         return {"sphere_block": list(sh.sphere_block), "sphere_grid": list(sh.sphere_grid),
                 "list_step_block": sh.list_step_block, "list_step_passes": sh.list_step_passes,
-                "list_build_block": sh.list_build_block}
+                "list_build_block": sh.list_build_block, "list_step_persistent": bool(sh.list_step_persistent)}
 
 
 # ---- fixture I/O (host functions of libbmxg.so; no device needed) -------------

@@ -494,9 +494,13 @@ typedef struct bmxg_shapes {
     int32_t list_step_block;    /* FP32F list step                                   */
     int32_t list_step_passes;   /* passes of the block per chunk (0: the size rule)  */
     int32_t list_build_block;   /* list build                                        */
-    int32_t reserved;
+    int32_t list_step_persistent; /* 1: one wave of blocks taking chunks from a counter */
 } bmxg_shapes;
 int  bmxg_get_shapes(const bmxg_ctx *ctx, bmxg_shapes *out);
+/* Use these shapes (blocks a multiple of 32 up to 256, grid >= 0, passes
+ * 0..64; else BMXG_ERR_ARG): pins what bmxg_autotune would pick.  The results
+ * of a step do not depend on the shapes. */
+int  bmxg_set_shapes(bmxg_ctx *ctx, const bmxg_shapes *in);
 
 #ifdef __cplusplus
 }

@@ -238,7 +238,7 @@ def test_autotune_list_shapes_leave_state_and_steps_unchanged(gpu_lib, tmp_path)
     A, B = ctx_for(w), ctx_for(w)
     A.autotune(cache)
     sh = A.shapes()
-    assert sh["list_step_block"] in (64, 128, 256) and sh["list_step_passes"] in (1, 2, 4)
+    assert sh["list_step_block"] in (64, 128, 256) and sh["list_step_passes"] in (1, 2, 4, 8)
     assert sh["list_build_block"] in (64, 128, 256)
     Q0 = read(A, w.particles)
     for k in ("x", "y", "z"):
@@ -276,5 +276,28 @@ def test_prepare_instantiates_graphs_and_changes_no_result(gpu_lib):
         QA, QB = read(A, w.particles), read(B, w.particles)
         for k in ("x", "y", "z", "velx", "vely", "velz"):
             assert np.array_equal(QA[k], QB[k]), (prec, k)
+    A.close()
+    B.close()
+
+
+@pytest.mark.parametrize("shape", [dict(list_step_persistent=True, list_step_passes=4),
+                                   dict(list_step_persistent=True, list_step_block=64, list_step_passes=8),
+                                   dict(list_step_block=256, list_step_passes=1, list_build_block=64)])
+def test_list_shapes_bitwise_same_steps(gpu_lib, shape):
+    """Every launch shape of the list step and build (one block per chunk, or
+    one persistent wave taking chunks from a counter) gives bit-identical
+    steps, the persistent dispenser resetting itself between launches."""
+    w = configs.colonies(ncol=12)
+    A, B = ctx_for(w), ctx_for(w)
+    A.set_shapes(**shape)
+    for c in (A, B):
+        c.step(w.dt, 24, BMXG_FP32F)
+        c.step(w.dt, 5, BMXG_FP32F)  # eager steps after the graph replays
+    assert A.stats()["n_rebins"] == B.stats()["n_rebins"] >= 1
+    QA, QB = read(A, w.particles), read(B, w.particles)
+    for k in ("x", "y", "z", "velx", "vely", "velz"):
+        assert np.array_equal(QA[k], QB[k]), k
+    with pytest.raises(Exception):
+        A.set_shapes(list_step_block=48)
     A.close()
     B.close()
