@@ -54,10 +54,32 @@ __device__ __forceinline__ double wall_slope(double z, double rS, const DevParam
     return 0.0;
 }
 
+// The FP32 screen of the FP64 pair walks (as in the FP64 sphere step): false
+// only when the candidate is certainly beyond the cutoff r_i + r_j + bw, from
+// the FP32 offsets to the bin corners with an absolute slack of 8 ulp of the
+// largest bin width that bounds their error; the FP64 gate decides the rest.
+__device__ __forceinline__ bool near32(const float4 me, const float4 q, int dxs, int dys, int dzs, const DevGeom &G,
+                                       float bwf, float slack)
+{
+    const float ex = (me.x - q.x) - (float)dxs * G.dxf[0];
+    const float ey = (me.y - q.y) - (float)dys * G.dxf[1];
+    const float ez = (me.z - q.z) - (float)dzs * G.dxf[2];
+    const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+    const float lim = __fadd_rn(__fadd_rn(__fadd_rn(me.w, q.w), bwf), slack);
+    return !(r2f > __fmul_rn(lim, lim));
+}
+
+__device__ __forceinline__ float screen_slack(const DevGeom &G)
+{
+    return 8.0f * 1.1920929e-7f * fmaxf(G.dxf[0], fmaxf(G.dxf[1], G.dxf[2]));
+}
+
 // forward step of the differentiable form (reads buffer a, writes b, rebins)
+template <bool SORTED>
 __global__ void __launch_bounds__(256) k_dfwd(const DevState S, const DevParams P, DiffParams D, double dt, int a)
 {
     const int b = a ^ 1;
+    const float bwf = P.bw32;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, i);
         int bx, by;
@@ -66,8 +88,13 @@ __global__ void __launch_bounds__(256) k_dfwd(const DevState S, const DevParams 
         const double ri = S.rad[i];
         const double mi = mobility_of(ri, D.mu);
         const double ai = D.adh ? D.adh[i] : 0.0;
+        const float4 me = S.rel[a][i];
+        const float slack = screen_slack(G);
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        visit_stencil(S, G, a, i, bx, by, S.iz[a][i], [&](int j, int, int, int, int sx, int sy) {
+        walk<SORTED>(S, G, a, i, bx, by, S.iz[a][i], [&](const float4 qr, auto slot, int dxs, int dys, int dzs,
+                                                         int sx, int sy) {
+            if (!near32(me, qr, dxs, dys, dzs, G, bwf, slack)) return;
+            const int j = slot();
             const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
             const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
             const double dx = xi - xj, dy = yi - yj, dz = zi - S.z[a][j];
@@ -103,11 +130,13 @@ __global__ void __launch_bounds__(256) k_dfwd(const DevState S, const DevParams 
 }
 
 // adjoint of the step taken from buffer a (positions x_t, bins of x_t)
+template <bool SORTED>
 __global__ void __launch_bounds__(256) k_dadj(const DevState S, const DevParams P, DiffParams D, double dt, int a,
                                              const double *__restrict__ lin, double *__restrict__ lout,
                                              double *__restrict__ gacc, double *__restrict__ gadh)
 {
     const int n = S.n;
+    const float bwf = P.bw32;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const DevGeom &G = geom_of(S, k);
         int bx, by;
@@ -120,7 +149,12 @@ __global__ void __launch_bounds__(256) k_dadj(const DevState S, const DevParams 
         const double lk[3] = {lin[k], lin[(size_t)n + k], lin[(size_t)2 * n + k]};
         double acc[3] = {0.0, 0.0, 0.0};
         double gk = 0.0, gg = 0.0, gm = 0.0, ga = 0.0;
-        visit_stencil(S, G, a, k, bx, by, S.iz[a][k], [&](int j, int, int, int, int sx, int sy) {
+        const float4 me = S.rel[a][k];
+        const float slack = screen_slack(G);
+        walk<SORTED>(S, G, a, k, bx, by, S.iz[a][k], [&](const float4 qr, auto slot, int dxs, int dys, int dzs,
+                                                         int sx, int sy) {
+            if (!near32(me, qr, dxs, dys, dzs, G, bwf, slack)) return;
+            const int j = slot();
             const double xj = sx ? S.x[a][j] + (double)sx * G.len[0] : S.x[a][j];
             const double yj = sy ? S.y[a][j] + (double)sy * G.len[1] : S.y[a][j];
             const double d[3] = {xk - xj, yk - yj, zk - S.z[a][j]};
@@ -189,14 +223,16 @@ __global__ void k_dreduce(const double *gacc, int n, int planes, double *out)
 int launch_dfwd(const DevState &S, const DevParams &P, const DiffParams &D, double dt, int a, int grid, int block,
                 cudaStream_t st)
 {
-    k_dfwd<<<grid, block, 0, st>>>(S, P, D, dt, a);
+    if (S.srel[a]) k_dfwd<true><<<grid, block, 0, st>>>(S, P, D, dt, a);
+    else k_dfwd<false><<<grid, block, 0, st>>>(S, P, D, dt, a);
     return 1;
 }
 
 int launch_dadj(const DevState &S, const DevParams &P, const DiffParams &D, double dt, int a, const double *lin,
                 double *lout, double *gacc, double *gadh, int grid, int block, cudaStream_t st)
 {
-    k_dadj<<<grid, block, 0, st>>>(S, P, D, dt, a, lin, lout, gacc, gadh);
+    if (S.srel[a]) k_dadj<true><<<grid, block, 0, st>>>(S, P, D, dt, a, lin, lout, gacc, gadh);
+    else k_dadj<false><<<grid, block, 0, st>>>(S, P, D, dt, a, lin, lout, gacc, gadh);
     return 1;
 }
 

@@ -266,7 +266,10 @@ __global__ void k_trig(const DevState S, int b)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
         const double th = S.theta[b][i], ph = S.phi[b][i];
-        S.trig[b][i] = make_trig(cos(th), sin(th), cos(ph), sin(ph));
+        double st, ct, sp, cp;
+        sincos(th, &st, &ct);
+        sincos(ph, &sp, &cp);
+        S.trig[b][i] = make_trig(ct, st, cp, sp);
     }
 }
 

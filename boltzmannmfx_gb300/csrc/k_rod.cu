@@ -795,7 +795,9 @@ __global__ void k_rod_update(const DevState S, double dt, int a)
             const double c = om[2], s = om[1];
             const double Q[3][3] = {{1.0, 0.0, 0.0}, {0.0, c, -s}, {0.0, s, c}};
             const double ang = on * dt;
-            const double u[3] = {cos(ang), sin(ang), 0.0};
+            double sa, ca;
+            sincos(ang, &sa, &ca);  // one argument reduction for both
+            const double u[3] = {ca, sa, 0.0};
             double q[3], nd[3];
             for (int r = 0; r < 3; ++r) {
                 q[r] = 0.0;
@@ -810,7 +812,10 @@ __global__ void k_rod_update(const DevState S, double dt, int a)
             if (rho > 0.0) nd[0] /= rho;
             ph = acos(nd[0]);
             if (nd[1] < 0.0) ph = 2.0 * kPi - ph;
-            tr = make_trig(cos(th), sin(th), cos(ph), sin(ph));
+            double st2, ct2, sp2, cp2;
+            sincos(th, &st2, &ct2);
+            sincos(ph, &sp2, &cp2);
+            tr = make_trig(ct2, st2, cp2, sp2);
         }
         S.theta[b][i] = th;
         S.phi[b][i] = ph;

@@ -31,24 +31,6 @@ namespace bmxg {
 
 namespace {
 
-// Walk the stencil over the column-sorted copies when the state has them
-// (SORTED), else over perm (callers that provide no sorted buffers).  f gets
-// the candidate's FP32 offsets, a functor returning its slot, and the shifts.
-template <bool SORTED, class F>
-__device__ __forceinline__ void walk(const DevState &S, const DevGeom &G, int a, int i, int bx, int by, int izi,
-                                     F &&f)
-{
-    if constexpr (SORTED) {
-        visit_sorted(S, G, a, S.rank[a][i], bx, by, izi, [&](int t, int dxs, int dys, int dzs, int sx, int sy) {
-            f(__ldg(&S.srel[a][t]), [&]() { return __ldg(&S.perm[a][t]); }, dxs, dys, dzs, sx, sy);
-        });
-    } else {
-        visit_stencil(S, G, a, i, bx, by, izi, [&](int j, int dxs, int dys, int dzs, int sx, int sy) {
-            f(__ldg(&S.rel[a][j]), [&]() { return j; }, dxs, dys, dzs, sx, sy);
-        });
-    }
-}
-
 // The FP64 pair term of slot i (at xi, yi, zi, radius ri, colony geometry
 // G) from neighbour j under image shift (sx, sy), in the reference's operation
 // order: false when the pair is not in the neighbour list or beyond the
