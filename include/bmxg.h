@@ -280,8 +280,8 @@ int  bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0,
  * Limits: n <= 32768 and n_cell[0] * n_cell[1] <= 65536, else
  * BMXG_ERR_CAPACITY.  The binning scratch is one fixed device array of about
  * 2.4 MB that every GPU loading the library holds until the process exits.
- * The first call on a device looks up that array's address; make that first
- * call before any stream capture.  Every call reuses the array: calls that
+ * The first call on a device looks up that array's address.  Every call
+ * reuses the array: calls that
  * overlap on the GPU (other streams, other host threads) race and must not
  * be issued.
  * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
