@@ -58,33 +58,48 @@ __device__ __forceinline__ bool sphere_term64(const DevState &S, const DevGeom &
     return true;
 }
 
-// FP64 plain step.  Each lane walks its slot's stencil and screens the
+// FP64 plain step.  Each thread walks its slot's stencil and screens the
 // candidates in FP32 (FP32 and integer work); the few that can pass the
 // cutoff (about 1.3 per slot on the colonies) are staged in shared memory,
-// and the warp then evaluates its slots' staged pairs together, one per lane,
-// so that the FP64 gate, square root and divisions run in full warps (GB300
-// issues FP64 at 2 lanes per clock per SM whatever the mask: a lane walking
-// its own candidates keeps 8 of 32 lanes busy in those instructions).  Each
-// slot then adds its pairs' terms in walk order -- the same FP64 values in
-// the same order as a walk that evaluates each pair when it meets it, so the
-// result stays bit-identical to the oracle.  A slot with more than kStage64
-// staged candidates evaluates them itself, in order, as it walks.
+// and the block then evaluates its slots' staged pairs together, one per
+// thread, so that the FP64 gate, square root and divisions run in full warps
+// (GB300 issues FP64 at 2 lanes per clock per SM whatever the mask: a thread
+// walking its own candidates keeps 8 of 32 lanes busy in those instructions),
+// and a warp whose share of a round is empty skips it.  Each slot then adds
+// its pairs' terms in walk order -- the same FP64 values in the same order as
+// a walk that evaluates each pair when it meets it, so the result stays
+// bit-identical to the oracle.  A slot with more than kStage64 staged
+// candidates evaluates them itself, in order, as it walks.
 constexpr int kStage64 = 16;
+
+// dynamic shared memory of k_sphere64 for a block of `block` threads
+__host__ __device__ constexpr size_t sphere64_smem(int block)
+{
+    return (size_t)block * (kStage64 * sizeof(int2) + 4 * sizeof(double) + 3 * sizeof(double) + 4 * sizeof(int)) +
+           2 * 32 * sizeof(int);
+}
 
 template <bool SORTED>
 __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevParams P, double dt, int a)
 {
-    // per warp: the lanes' staged candidates (j, image code), then one round's
-    // terms (dynamic shared memory, sized by the launcher)
-    extern __shared__ unsigned char sm64[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int2 *stage = reinterpret_cast<int2 *>(sm64) + (size_t)w * 32 * kStage64;
-    double *term = reinterpret_cast<double *>(sm64 + (size_t)(blockDim.x >> 5) * 32 * kStage64 * sizeof(int2)) +
-                   (size_t)w * 3 * 32;
+    // per thread: its staged candidates (j, image code); its slot's position,
+    // radius, colony and run of staged pairs (for the block's evaluation);
+    // one round's terms and gate results
+    extern __shared__ __align__(16) unsigned char sm64[];
+    const int B = blockDim.x, tid = threadIdx.x;
+    const int lane = tid & 31, w = tid >> 5, nw = B >> 5;
+    int2 *stage = reinterpret_cast<int2 *>(sm64);
+    double *opos = reinterpret_cast<double *>(stage + (size_t)B * kStage64);  // 4 per thread: x, y, z, r
+    double *term = opos + 4 * B;                                               // 3 per thread
+    int *ocol = reinterpret_cast<int *>(term + 3 * B);
+    int *orun = ocol + B;   // first staged pair of the slot in the block's run
+    int *olen = orun + B;   // its staged pairs
+    int *opass = olen + B;  // the round's gate result per thread
+    int *wsum = opass + B;  // per warp: staged pairs, then their exclusive scan
     const int b = a ^ 1;
     const float bwf = (float)P.bw;  // once per thread: a conversion is an FP64-pipe instruction
-    for (int base = blockIdx.x * blockDim.x; base < S.n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
+    for (int base = blockIdx.x * B; base < S.n; base += gridDim.x * B) {
+        const int i = base + tid;
         const bool act = i < S.n;
         double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
         double fx = 0.0, fy = 0.0, fz = 0.0;
@@ -103,7 +118,7 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
             const float dxb = G.dxf[0], dyb = G.dxf[1], dzb = G.dxf[2];
             // absolute slack bounding the FP32 distance error (offsets + bin widths)
             const float slack = 8.0f * 1.1920929e-7f * fmaxf(dxb, fmaxf(dyb, dzb));
-            int2 *mine = stage + lane * kStage64;
+            int2 *mine = stage + (size_t)tid * kStage64;
             auto eval = [&](int j, int sx, int sy) {
                 double t[3];
                 if (sphere_term64(S, G, P, a, xi, yi, zi, ri, j, sx, sy, t)) {
@@ -131,45 +146,64 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
                 ++cnt;
             });
         }
-        // the warp's staged pairs, one per lane
+        // the block's run of staged pairs: slot by slot in thread order
         const int xl = (cnt <= kStage64) ? cnt : 0;
         int xo = xl;
         for (int d = 1; d < 32; d <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, xo, d);
             if (lane >= d) xo += v;
         }
-        const int xt = __shfl_sync(0xffffffffu, xo, 31);
-        xo -= xl;
-        for (int t0 = 0; t0 < xt; t0 += 32) {
-            const int t = t0 + lane;
-            int o = 0;  // the slot that owns pair t: the last lane whose run starts at or before t
-            for (int s2 = 16; s2 >= 1; s2 >>= 1) {
-                const int v = __shfl_sync(0xffffffffu, xo, o + s2);
-                if (v <= t) o += s2;
+        if (lane == 31) wsum[w] = xo;
+        opos[4 * tid] = xi;
+        opos[4 * tid + 1] = yi;
+        opos[4 * tid + 2] = zi;
+        opos[4 * tid + 3] = ri;
+        ocol[tid] = col;
+        olen[tid] = xl;
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int v = 0; v < nw; ++v) {
+                const int c = wsum[v];
+                wsum[32 + v] = run;
+                run += c;
             }
-            const double oxi = __shfl_sync(0xffffffffu, xi, o), oyi = __shfl_sync(0xffffffffu, yi, o);
-            const double ozi = __shfl_sync(0xffffffffu, zi, o), ori = __shfl_sync(0xffffffffu, ri, o);
-            const int oc = __shfl_sync(0xffffffffu, col, o);
-            const int oxo = __shfl_sync(0xffffffffu, xo, o);
-            bool pass = false;
+            wsum[31] = run;  // (nw <= 8: slot 31 is free) the block's total
+        }
+        __syncthreads();
+        const int xt = wsum[31];
+        xo += wsum[32 + w] - xl;
+        orun[tid] = xo;
+        __syncthreads();
+        for (int t0 = 0; t0 < xt; t0 += B) {
+            const int t = t0 + tid;
+            int pass = 0;
             double tt[3] = {0.0, 0.0, 0.0};
-            if (t < xt) {
-                const int2 e = stage[o * kStage64 + (t - oxo)];
-                pass = sphere_term64(S, S.geoms[oc], P, a, oxi, oyi, ozi, ori, e.x, e.y / 3 - 1, e.y % 3 - 1, tt);
+            if (t0 + 32 * w < xt) {  // a warp with no pair in this round skips it
+                if (t < xt) {
+                    int o = 0;  // the slot that owns pair t: the last thread whose run starts at or before t
+                    for (int s2 = 1 << (31 - __clz(max(B - 1, 1))); s2 >= 1; s2 >>= 1)
+                        if (o + s2 < B && orun[o + s2] <= t) o += s2;
+                    const int2 e = stage[(size_t)o * kStage64 + (t - orun[o])];
+                    pass = sphere_term64(S, S.geoms[ocol[o]], P, a, opos[4 * o], opos[4 * o + 1], opos[4 * o + 2],
+                                         opos[4 * o + 3], e.x, e.y / 3 - 1, e.y % 3 - 1, tt)
+                               ? 1
+                               : 0;
+                }
             }
-            const unsigned pm = __ballot_sync(0xffffffffu, pass);
-            term[lane] = tt[0];
-            term[32 + lane] = tt[1];
-            term[64 + lane] = tt[2];
-            __syncwarp();
-            const int k1 = min(xo + xl, t0 + 32);
+            term[3 * tid] = tt[0];
+            term[3 * tid + 1] = tt[1];
+            term[3 * tid + 2] = tt[2];
+            opass[tid] = pass;
+            __syncthreads();
+            const int k1 = min(xo + xl, t0 + B);
             for (int k = max(xo, t0); k < k1; ++k) {
-                if (!((pm >> (k - t0)) & 1u)) continue;
-                fx += term[k - t0];
-                fy += term[32 + k - t0];
-                fz += term[64 + k - t0];
+                if (!opass[k - t0]) continue;
+                fx += term[3 * (k - t0)];
+                fy += term[3 * (k - t0) + 1];
+                fz += term[3 * (k - t0) + 2];
             }
-            __syncwarp();
+            __syncthreads();
         }
         if (act) {
             const DevGeom &G = S.geoms[col];
@@ -190,6 +224,7 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
             S.vz[i] = vz;
             rebin_slot(S, G, i, nx, ny, nz, ri, b);
         }
+        __syncthreads();  // the next pass reuses the stage and the slot records
     }
 }
 
@@ -280,15 +315,35 @@ __global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevPar
 
 }  // namespace
 
+// k_sphere64's dynamic shared memory above the default 48 KB for 256-thread
+// blocks: the attribute, once per device
+template <bool SORTED>
+void allow_sphere64_smem()
+{
+    static unsigned long long done = 0ull;  // a bit per device (set twice at worst: idempotent)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    if (dev < 64 && ((done >> dev) & 1ull)) return;
+    if (cudaFuncSetAttribute(k_sphere64<SORTED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sphere64_smem(256)) == cudaSuccess &&
+        dev < 64)
+        done |= 1ull << dev;
+}
+
 int launch_sphere_step(const DevState &S, const DevParams &P, double dt, int a, int precision, int grid,
                        int block, cudaStream_t st, int resync)
 {
     const bool sorted = S.srel[a] != nullptr;  // the context keeps sorted copies; bare callers do not
     if (precision == BMXG_FP64_FORM) {
-        // (block a multiple of 32: the warps stage and evaluate their pairs together)
-        const size_t smem = (size_t)(block / 32) * 32 * (kStage64 * sizeof(int2) + 3 * sizeof(double));
-        if (sorted) k_sphere64<true><<<grid, block, smem, st>>>(S, P, dt, a);
-        else k_sphere64<false><<<grid, block, smem, st>>>(S, P, dt, a);
+        // (block a multiple of 32, at most 256: the block stages and evaluates its pairs together)
+        const size_t smem = sphere64_smem(block);
+        if (sorted) {
+            allow_sphere64_smem<true>();
+            k_sphere64<true><<<grid, block, smem, st>>>(S, P, dt, a);
+        } else {
+            allow_sphere64_smem<false>();
+            k_sphere64<false><<<grid, block, smem, st>>>(S, P, dt, a);
+        }
     } else {
         if (sorted) k_sphere32<true><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
         else k_sphere32<false><<<grid, block, 0, st>>>(S, P, (float)dt, a, resync);
