@@ -429,6 +429,9 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
     const int i0 = ck * chunk;
     const int i1 = min(i0 + chunk, n);
     int colony = (i0 + (int)threadIdx.x < i1) ? colony_of(S.cbase, S.ncol, i0 + threadIdx.x) : 0;
+    // the first slot of the next colony, kept in a register: the common step
+    // compares against it instead of loading it
+    int cnext = (colony + 1 < S.ncol) ? __ldg(&S.cbase[colony + 1]) : 0x7fffffff;
     for (int base = i0; base < i1; base += blockDim.x) {  // same trip count for every thread
         const int i = base + threadIdx.x;
         const bool act = i < i1;
@@ -466,7 +469,10 @@ __global__ void __launch_bounds__(256, 6) k_list_step(const DevState S, const De
         };
         int4 rec = make_int4(0, 0, 0, 0);
         if (act) {
-            while (colony + 1 < S.ncol && __ldg(&S.cbase[colony + 1]) <= i) ++colony;
+            while (i >= cnext) {
+                ++colony;
+                cnext = (colony + 1 < S.ncol) ? __ldg(&S.cbase[colony + 1]) : 0x7fffffff;
+            }
             rec = __ldg(&S.lrec[i]);
             h = ga[i];
             cnt = rec.x & 0xff;
