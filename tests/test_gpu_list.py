@@ -280,6 +280,25 @@ def test_prepare_instantiates_graphs_and_changes_no_result(gpu_lib):
     B.close()
 
 
+def test_prepare_rods_fp32f_pipeline(gpu_lib):
+    """bmxg_prepare on a rod state allocates the FP32F rod pipeline and captures
+    its graphs: the steps after it equal those of an unprepared context."""
+    w = configs.rod_trees(ntrees=40, per_tree=50)
+    A, B = Context(w.params, w.geoms), Context(w.params, w.geoms)
+    for c in (A, B):
+        c.set_state(w.particles, w.offsets)
+    A.prepare(w.dt, BMXG_FP32F)
+    for c in (A, B):
+        c.step(w.dt, 20, BMXG_FP32F)
+    QA, QB = w.particles.copy(), w.particles.copy()
+    A.get_state(QA)
+    B.get_state(QB)
+    for k in ("x", "y", "z", "theta", "phi", "velx", "vely", "velz", "wx", "wy", "wz"):
+        assert np.array_equal(QA[k], QB[k]), k
+    A.close()
+    B.close()
+
+
 @pytest.mark.parametrize("shape", [dict(list_step_persistent=True, list_step_passes=4),
                                    dict(list_step_persistent=True, list_step_block=64, list_step_passes=8),
                                    dict(list_step_block=256, list_step_passes=1, list_build_block=64)])

@@ -137,3 +137,43 @@ def test_tile_rejects_reals_outside_and_non_spheres(gpu_lib):
     with pytest.raises(BmxgError):  # not a box of the domain
         ctx.step_tile((0, 0, 0), (64, 31, 31), take(P, idx), G, 0.25)
     ctx.close()
+
+
+def test_tile_on_device_arrays(gpu_lib):
+    """The same tile call with every array in device memory (where = BMXG_DEVICE)."""
+    import ctypes as C
+    import torch
+    from boltzmannmfx_gb300 import abi
+    prm, g, P = workload(n=5_000)
+    lo, hi = (0, 0, 0), (31, 31, 31)
+    idx, R, G = tile_inputs(g, P, lo, hi)
+    ctx = Context(prm, [g])
+    Rh = take(P, idx)
+    ctx.step_tile(lo, hi, Rh, G, 0.25)          # host arrays: the expected result
+    dev = {}
+
+    def to_dev(Q, fields):
+        s = abi.ParticlesStruct()
+        s.n = Q.n
+        for name, ctype in abi.ParticlesStruct._fields_[1:]:
+            if name in fields:
+                t = torch.from_numpy(np.ascontiguousarray(Q[name])).cuda()
+                dev[(id(Q), name)] = t
+                setattr(s, name, C.cast(C.c_void_p(t.data_ptr()), ctype))
+            else:
+                setattr(s, name, ctype())
+        return s
+
+    Rd = take(P, idx)
+    sr = to_dev(Rd, ("x", "y", "z", "radius", "cell_type", "velx", "vely", "velz"))
+    sg = to_dev(G, ("x", "y", "z", "radius", "cell_type"))
+    t = abi.Tile()
+    t.lo[:] = list(lo)
+    t.hi[:] = list(hi)
+    rc = ctx.lib.bmxg_step_tile(ctx.h, C.byref(t), C.byref(sr), C.byref(sg), 0.25, abi.BMXG_DEVICE)
+    assert rc == abi.BMXG_OK, ctx.lib.bmxg_last_error(ctx.h)
+    torch.cuda.synchronize()
+    for k in OUT:
+        got = dev[(id(Rd), k)].cpu().numpy()
+        assert np.array_equal(got, Rh[k]), k
+    ctx.close()
