@@ -1416,7 +1416,7 @@ int bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *r
                     alloc(&B.ox, nr) && alloc(&B.oy, nr) && alloc(&B.oz, nr) && alloc(&B.vx, nr) &&
                     alloc(&B.vy, nr) && alloc(&B.vz, nr) && alloc(&B.cell, nt) && alloc(&B.cnt, ncells) &&
                     alloc(&B.start, ncells + 1) && alloc(&B.fill, ncells) && alloc(&B.perm, nt) &&
-                    alloc(&B.bad, 2) && alloc(&scratch, scan_scratch_ints((int)ncells));
+                    alloc(&B.bad, 3) && alloc(&scratch, scan_scratch_ints((int)ncells));
     if (!ok) {
         release();
         (void)cudaGetLastError();
@@ -1442,15 +1442,15 @@ int bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *r
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(B.cnt, 0, sizeof(int) * ncells, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.fill, 0, sizeof(int) * ncells, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(B.bad, 0, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.bad, 0, 3 * sizeof(unsigned long long), st);
     if (e == cudaSuccess) {
         ctx->launches += launch_tile_step(B, T, dev_params(ctx->prm), dt / 1.0, (int)nr, (int)nt, scratch, ctx->nsm, st);
         e = cudaGetLastError();
     }
-    unsigned long long bad[2] = {0ull, 0ull};
+    unsigned long long bad[3] = {0ull, 0ull, 0ull};
     if (e == cudaSuccess) e = cudaMemcpyAsync(bad, B.bad, sizeof(bad), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess && !bad[0] && !bad[1]) {
+    if (e == cudaSuccess && !bad[0] && !bad[1]) {  // (non-finite positions are written, then reported)
         auto out = [&](void *dst, const void *src) {
             if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, 8 * nr, kout, st);
         };
@@ -1467,6 +1467,7 @@ int bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *r
     if (bad[1]) return fail(ctx, BMXG_ERR_UNSUPPORTED, "the tile step takes spheres (YEAST) only");
     if (bad[0])
         return fail(ctx, BMXG_ERR_ARG, "a real particle outside the tile or a ghost outside its one-cell halo");
+    if (bad[2]) return fail(ctx, BMXG_ERR_NONFINITE, "a tile step produced a non-finite position");
     return BMXG_OK;
 }
 

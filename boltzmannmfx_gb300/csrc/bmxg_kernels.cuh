@@ -235,7 +235,8 @@ struct TileBufs {
     int *ct;
     double *ox, *oy, *oz, *vx, *vy, *vz;
     int *cell, *cnt, *start, *fill, *perm;
-    unsigned long long *bad;  // [2]: a real outside the tile or a ghost outside the halo; a non-sphere
+    unsigned long long *bad;  // [3]: a real outside the tile or a ghost outside the halo; a non-sphere;
+                              // a non-finite new position
 };
 // bin, count, scan, scatter, order each cell by index, step the reals
 int launch_tile_step(const TileBufs &B, const TileGeom &T, const DevParams &P, double dt, int nreal, int ntot,

@@ -91,7 +91,8 @@ __global__ void __launch_bounds__(128) k_tile_step(const double *__restrict__ x,
                                                    int nreal, const int *__restrict__ cell,
                                                    const int *__restrict__ start, const int *__restrict__ perm,
                                                    TileGeom T, DevParams P, double dt, double *ox, double *oy,
-                                                   double *oz, double *vx, double *vy, double *vz)
+                                                   double *oz, double *vx, double *vy, double *vz,
+                                                   unsigned long long *bad)
 {
     const int nz2 = T.nt[2] + 2, nyz = (T.nt[1] + 2) * nz2;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nreal; i += gridDim.x * blockDim.x) {
@@ -142,6 +143,7 @@ __global__ void __launch_bounds__(128) k_tile_step(const double *__restrict__ x,
         const double nz = zi + dt * v2;
         if (T.per[0]) nx = wrap1(nx, T.plo[0], T.phi[0], T.len[0]);
         if (T.per[1]) ny = wrap1(ny, T.plo[1], T.phi[1], T.len[1]);
+        if (!finite_bits(nx) || !finite_bits(ny) || !finite_bits(nz)) atomicAdd(&bad[2], 1ull);
         ox[i] = nx;
         oy[i] = ny;
         oz[i] = nz;
@@ -165,7 +167,7 @@ int launch_tile_step(const TileBufs &B, const TileGeom &T, const DevParams &P, d
     k_tile_scatter<<<gp, blk, 0, st>>>(B.cell, ntot, B.start, B.fill, B.perm);
     k_tile_order<<<gc, blk, 0, st>>>(B.start, ncells, B.perm);
     k_tile_step<<<std::max(1, std::min((nreal + 127) / 128, nsm * 16)), 128, 0, st>>>(
-        B.x, B.y, B.z, B.r, nreal, B.cell, B.start, B.perm, T, P, dt, B.ox, B.oy, B.oz, B.vx, B.vy, B.vz);
+        B.x, B.y, B.z, B.r, nreal, B.cell, B.start, B.perm, T, P, dt, B.ox, B.oy, B.oz, B.vx, B.vy, B.vz, B.bad);
     return k + 3;
 }
 

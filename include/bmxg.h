@@ -483,7 +483,8 @@ typedef struct bmxg_tile {
  * where: BMXG_HOST or BMXG_DEVICE for every array.  Returns BMXG_ERR_ARG when
  * a real particle is outside the tile or a ghost outside its one-cell halo,
  * BMXG_ERR_UNSUPPORTED for a particle that is not YEAST (rod segments need
- * their neighbours' bond tables: a whole-domain step). */
+ * their neighbours' bond tables: a whole-domain step), BMXG_ERR_NONFINITE
+ * (after writing the results) when a new position is not finite. */
 int  bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *reals,
                     const bmxg_particles *ghosts, double dt, int32_t where);
 

@@ -136,6 +136,11 @@ def test_tile_rejects_reals_outside_and_non_spheres(gpu_lib):
         ctx.step_tile((0, 0, 0), (31, 31, 31), R3, G, 0.25)
     with pytest.raises(BmxgError):  # not a box of the domain
         ctx.step_tile((0, 0, 0), (64, 31, 31), take(P, idx), G, 0.25)
+    R5 = take(P, idx)
+    R5["z"][0] = np.nan             # a non-finite position comes back as an error, as from bmxg_step
+    with pytest.raises(BmxgError) as e:
+        ctx.step_tile((0, 0, 0), (31, 31, 31), R5, G, 0.25)
+    assert "non-finite" in str(e.value)
     ctx.close()
 
 
