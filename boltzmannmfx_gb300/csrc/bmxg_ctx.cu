@@ -961,14 +961,17 @@ int ensure_list(bmxg_ctx *ctx, float skin)
             if ((rc = dalloc(ctx, &S.fxh[k], ctx->n))) return rc;
             if ((rc = dalloc(ctx, &S.fxl[k], 3 * (size_t)ctx->n))) return rc;
         }
-        if ((rc = dalloc(ctx, &S.cellcnt, ctx->ncells_total))) return rc;
+        if ((rc = dalloc(ctx, &S.lkey, ctx->n))) return rc;
         if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
-        // (the scratch serves the scan of the cell counts and that of the groups' entries)
-        const int nscan = (int)std::max<int64_t>(ctx->ncells_total, ((int64_t)ctx->n + 31) / 32);
+        // (the scratch serves the scan of the column counts and that of the groups' entries)
+        const int nscan = (int)std::max<int64_t>(S.ncols_total, ((int64_t)ctx->n + 31) / 32);
         if ((rc = dalloc(ctx, &ctx->cell_scratch, scan_scratch_ints(nscan)))) return rc;
         if ((rc = dalloc(ctx, &S.lctl, 1))) return rc;
         S.ncells_total = (int)ctx->ncells_total;
-        CK(cudaMemsetAsync(S.cellcnt, 0, sizeof(int) * ctx->ncells_total, ctx->stream));
+        S.cols_max = 0;
+        for (const DevGeom &g : ctx->h_geoms) S.cols_max = std::max(S.cols_max, g.n[0] * g.n[1]);
+        // offsets within [0, n] from the start, whatever a build leaves unwritten
+        CK(cudaMemsetAsync(S.cellstart, 0, sizeof(int) * (ctx->ncells_total + 1), ctx->stream));
         ctx->list_valid = false;
         drop_graphs(ctx);  // captured kernels hold the state's pointers by value
     }

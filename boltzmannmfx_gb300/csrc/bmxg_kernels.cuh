@@ -135,9 +135,11 @@ struct DevState {
     const FxGeom *fxg; // per colony
     int *pcap;         // null, or per slot 1 + kPairCap ints: the gated pairs of the last
                        // list step (count, then neighbour slots in accumulation order)
-    int *cellcnt;      // per 3D cell counter, zero between uses
+    unsigned long long *lkey;  // build scratch, n: at each column position the counting sort
+                               // gave a slot, that slot's (z bin, caller index) key
     int *cellstart;    // ncells_total + 1 offsets of the cells in the sorted copies
     int ncells_total;
+    int cols_max;      // largest column count of a colony
     ListCtl *lctl;
 };
 
@@ -210,7 +212,7 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
                         int build_block, cudaStream_t st);
 // the list build kernel alone (gated on lctl->rebuild), build_block threads per block
 int launch_list_build(const DevState &S, const DevParams &P, int build_block, cudaStream_t st);
-constexpr int kListBodyKernels = 12;
+constexpr int kListBodyKernels = 13;
 // force + wall + update over the list, reading buffer a and writing buffer b
 // (grid = the SM count; passes of the block per chunk of slots, <= 0: a rule;
 // persistent: one wave of blocks taking chunks from a counter, else one block

@@ -169,7 +169,7 @@ __device__ __forceinline__ int fx_bin(unsigned h, int nb, int per)
 }
 
 // Bins of buffer a's fixed-point positions into the list bins (kListBins
-// buffer) and the 3D cell counts.
+// buffer) and the column counts.
 __global__ void k_list_rebin(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
@@ -184,55 +184,53 @@ __global__ void k_list_rebin(const DevState S, int a)
         const int bx = fx_bin((unsigned)h.x, F.n[0], F.per[0]);
         const int by = fx_bin((unsigned)h.y, F.n[1], F.per[1]);
         const int bz = fx_bin((unsigned)h.z, F.n[2], F.per[2]);
-        S.col[B][i] = column_of(G, bx, by);
+        const int c = column_of(G, bx, by);
+        S.col[B][i] = c;
         S.iz[B][i] = bz;
-        atomicAdd(&S.cellcnt[cell_of(G, bx, by, bz)], 1);
+        atomicAdd(&S.colcnt[c], 1);
     }
 }
 
-// counting sort into the cells (arrival order from the atomics)
+// The order key of a slot inside its column: z bin, then caller index (the
+// sorted order is column, z bin, caller index, as the 3D cells hold it).
+__device__ __forceinline__ unsigned long long list_key(int bz, int orig)
+{
+    return ((unsigned long long)(unsigned)bz << 32) | (unsigned)orig;
+}
+
+// counting sort into the columns (arrival order from the atomics): each slot's
+// key at the position it drew
 __global__ void k_list_scatter(const DevState S)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int col = block_colony(S, i);
     if (i < S.n) {
-        const DevGeom &G = S.geoms[col];
-        int bx, by;
-        col_to_bxy(G, S.col[B][i], bx, by);
-        const int c = cell_of(G, bx, by, S.iz[B][i]);
-        const int r = atomicSub(&S.cellcnt[c], 1) - 1;  // leaves cellcnt at zero
-        const int t = S.cellstart[c] + r;
-        if (t >= 0 && t < S.n) S.tmp[t] = i;
+        const int c = S.col[B][i];
+        const int r = atomicSub(&S.colcnt[c], 1) - 1;  // leaves colcnt at zero
+        const int t = S.colstart[B][c] + r;
+        if (t >= 0 && t < S.n) S.lkey[t] = list_key(S.iz[B][i], S.orig[i]);
         else atomicAdd(&S.cnt->bad_index, 1ULL);
     }
 }
 
-// deterministic order inside a cell (ascending original index), and the
-// sorted copies the build walks: the position record, z bin, slot, and each
-// slot's rank
+// deterministic order inside a column (z bin, then ascending original index:
+// the slot's rank among its column's keys), and the sorted copies the build
+// walks: the position record, z bin, slot, and each slot's rank
 __global__ void k_list_canon(const DevState S, int a)
 {
     if (!S.lctl->rebuild) return;
     constexpr int B = kListBins;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int col = block_colony(S, i);
     if (i < S.n) {
-        const DevGeom &G = S.geoms[col];
-        int bx, by;
-        col_to_bxy(G, S.col[B][i], bx, by);
+        const int c = S.col[B][i];
         const int bz = S.iz[B][i];
-        const int c = cell_of(G, bx, by, bz);
-        const int s0 = max(S.cellstart[c], 0), s1 = min(S.cellstart[c + 1], S.n);
-        const int oi = S.orig[i];
+        const int s0 = max(S.colstart[B][c], 0), s1 = min(S.colstart[B][c + 1], S.n);
+        const unsigned long long me = list_key(bz, S.orig[i]);
         int rank = 0;
-        for (int t = s0; t < s1; ++t) {
-            const int j = S.tmp[t];
-            if ((unsigned)j < (unsigned)S.n) rank += (S.orig[j] < oi);
-        }
+        for (int t = s0; t < s1; ++t) rank += (__ldg(&S.lkey[t]) < me);
         const int t = s0 + rank;
-        if (t >= s1) {  // i is not among its cell's members: inconsistent counts
+        if (t >= s1) {  // i is not among its column's members: inconsistent counts
             atomicAdd(&S.cnt->bad_index, 1ULL);
         } else {
             S.perm[B][t] = i;
@@ -241,6 +239,63 @@ __global__ void k_list_canon(const DevState S, int a)
             S.rank[B][i] = t;
         }
     }
+}
+
+// The 3D cells' offsets in the sorted copies from the columns' sorted z bins:
+// cell (column, z) starts at the column's first position whose z bin is z or
+// more.  One thread per column of the colony blockIdx.x (kCellsBlock columns
+// per block, blocks strided over blockIdx.y) walks its column's members once
+// and leaves the offsets of kCellsZ z bins at a time in shared memory; the
+// block then writes its columns' cells, which lie together, in whole rows.
+// The last entry (one past the last cell) is n.
+constexpr int kCellsBlock = 128;
+constexpr int kCellsZ = 32;  // one z bin per lane in the write-out
+
+__global__ void __launch_bounds__(kCellsBlock) k_list_cells(const DevState S)
+{
+    if (!S.lctl->rebuild) return;
+    constexpr int B = kListBins;
+    constexpr int R = kCellsZ + 1;  // row pitch (no bank conflicts between the columns' rows)
+    __shared__ int off[kCellsBlock * R];
+    const DevGeom &G = S.geoms[blockIdx.x];
+    const int nz = G.n[2];
+    const int ncols = G.n[0] * G.n[1];
+    for (int q0 = blockIdx.y * kCellsBlock; q0 < ncols; q0 += gridDim.y * kCellsBlock) {  // same trip count
+        const int q = q0 + threadIdx.x;
+        const int nq = min(kCellsBlock, ncols - q0);
+        // t: the column's first position whose z bin (v; past the column's
+        // end: above every bin) is not below the current z
+        int t = 0, s1 = 0;
+        if (q < ncols) {
+            t = max(__ldg(&S.colstart[B][G.col_base + q]), 0);
+            s1 = min(__ldg(&S.colstart[B][G.col_base + q + 1]), S.n);
+        }
+        int v = (t < s1) ? __ldg(&S.siz[B][t]) : 0x7fffffff;
+        for (int zc = 0; zc < nz; zc += kCellsZ) {
+            const int zl = min(kCellsZ, nz - zc);
+            if (q < ncols) {
+                for (int k = 0; k < zl; ++k) {
+                    const int z = zc + k + 1;
+                    while (v < z) {
+                        ++t;
+                        v = (t < s1) ? __ldg(&S.siz[B][t]) : 0x7fffffff;
+                    }
+                    off[threadIdx.x * R + k] = t;
+                }
+            }
+            __syncthreads();
+            // the block's cells of this z range: a warp writes one column's zl
+            // cells at a time, lane k the k-th (a whole row; the columns' rows
+            // lie one after another when nz <= kCellsZ)
+            const int lane = threadIdx.x & 31;
+            int *dst = S.cellstart + G.cell_base + (size_t)q0 * nz + zc;
+            if (lane < zl)
+                for (int cq = threadIdx.x >> 5; cq < nq; cq += kCellsBlock / 32)
+                    dst[(size_t)cq * nz + lane] = off[cq * R + lane];
+            __syncthreads();
+        }
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) S.cellstart[S.ncells_total] = S.n;
 }
 
 // Visit the slots of the 3 x 3 neighbour columns of bin (bx, by), z bins
@@ -767,9 +822,12 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     // one slot per thread (a block's colonies from one search)
     const int g1 = (S.n + block - 1) / block;
     k_list_rebin<<<g1, block, 0, st>>>(S, a);
-    int k = 1 + launch_scan(S.cellcnt, S.cellstart, S.ncells_total, scan_scratch, st, gate);
+    int k = 1 + launch_scan(S.colcnt, S.colstart[kListBins], S.ncols_total, scan_scratch, st, gate);
     k_list_scatter<<<g1, block, 0, st>>>(S);
     k_list_canon<<<g1, block, 0, st>>>(S, a);
+    // the cell offsets: up to 64 blocks of columns per colony
+    const dim3 gc(S.ncol, std::max(1, std::min(64, (S.cols_max + kCellsBlock - 1) / kCellsBlock)));
+    k_list_cells<<<gc, kCellsBlock, 0, st>>>(S);
     // the build: one slot per thread in small blocks (the stencil walks
     // differ in length from slot to slot; small blocks on a grid of every
     // slot let the scheduler balance them)
@@ -779,7 +837,7 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     k_list_xcount<<<gx, 128, 0, st>>>(S);
     k = k + launch_scan(S.xcnt, S.xoff, (S.n + 31) / 32, scan_scratch, st, gate);
     k_list_xcopy<<<gx, 128, 0, st>>>(S);
-    return k + 5;
+    return k + 6;
 }
 
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,
