@@ -101,6 +101,8 @@ struct bmxg_ctx {
     double traj_dt = 0.0;
 
     bool vel32 = false;       // the last step's velocities are in the FP32F buffers
+    bool vel64_zero = false;  // the FP64 velocity planes (vx .. wz) hold zeros: a load zeroed them
+                              // and no kernel that writes them ran since
     int64_t step_count = 0;   // steps since set_state (FP32F re-sync schedule)
 
     // FP32F neighbour list with a skin (k_list.cu)
@@ -126,7 +128,7 @@ struct bmxg_ctx {
     // with the sort, gather and scatter kernels on `stream`; the device
     // staging is kept (and grown) across calls
     cudaStream_t io_stream = nullptr;
-    cudaEvent_t io_ev[6] = {};
+    cudaEvent_t io_ev[8] = {};
     char *io_buf = nullptr;
     size_t io_cap = 0;
     unsigned long long *d_chk = nullptr;    // state-check flags (4), device
@@ -532,10 +534,28 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
             if (off[c + 1] < off[c]) return fail(ctx, BMXG_ERR_ARG, "colony_offsets must not decrease");
     }
     const cudaMemcpyKind kind = (where == BMXG_HOST) ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    // A load of exactly the state the device holds (a caller that stores the
+    // state after a step and loads it back unchanged before the next, as a
+    // load-step-store loop does) keeps the slot order, the neighbour list and
+    // its frozen frames: the loaded positions, radii and cell types are
+    // compared bit for bit with the device state first (a state that passed
+    // the checks below before).  Only for spheres and when the caller gives no
+    // other field (which would overwrite device fields); what any load resets
+    // is reset here as well.
+    const bool only_required = !p->velx && !p->vely && !p->velz && !p->wx && !p->wy && !p->wz &&
+                               !p->c_length && !p->theta && !p->phi && !p->area && !p->bond_scale &&
+                               !p->id && !p->cpu && !p->n_bnds && !p->seg_id1 && !p->seg_id2 && !p->site &&
+                               !p->position && !p->fuse_tip && !p->fix_site && !p->fuse_flag &&
+                               !p->split_flag && !p->new_flag && !p->dltd;
+    const bool same_cand = n && only_required && ctx->have_state && ctx->n == n && ctx->offsets == off &&
+                           !ctx->S.has_rods;
+    // the comparison reads the device's FP64 positions
+    if (same_cand)
+        if (int rc = sync_fp64(ctx)) return rc;
     // Positions, radii and cell types: read in place from device arrays; host
     // arrays go to the staging, radii and cell types first on the compute
-    // stream (the state check needs them), positions on the copy stream, so
-    // that their copy overlaps the check and the host's decisions below.
+    // stream (the state checks need them), positions on the copy stream, so
+    // that their copy overlaps the checks and the host's decisions below.
     const double *src_x = p->x, *src_y = p->y, *src_z = p->z, *src_r = p->radius;
     const int *src_ct = p->cell_type;
     JoinIo join{nullptr};
@@ -551,7 +571,9 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         CK(cudaMemcpyAsync(br, p->radius, sizeof(double) * n, kind, st0));
         CK(cudaMemcpyAsync(bct, p->cell_type, sizeof(int) * n, kind, st0));
         CK(cudaMemcpyAsync(bx, p->x, sizeof(double) * n, kind, st1));
+        CK(cudaEventRecord(ctx->io_ev[6], st1));
         CK(cudaMemcpyAsync(by, p->y, sizeof(double) * n, kind, st1));
+        CK(cudaEventRecord(ctx->io_ev[7], st1));
         CK(cudaMemcpyAsync(bz, p->z, sizeof(double) * n, kind, st1));
         CK(cudaEventRecord(ctx->io_ev[1], st1));
         src_x = bx;
@@ -560,34 +582,38 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         src_r = br;
         src_ct = bct;
     }
-    // A load of exactly the state the device holds (a caller that stores the
-    // state after a step and loads it back unchanged before the next, as a
-    // load-step-store loop does) keeps the slot order, the neighbour list and
-    // its frozen frames: the loaded positions, radii and cell types are
-    // compared bit for bit with the device state first (a state that passed
-    // the checks below before).  Only for spheres and when the caller gives no
-    // other field (which would overwrite device fields); what any load resets
-    // is reset here as well.
-    const bool only_required = !p->velx && !p->vely && !p->velz && !p->wx && !p->wy && !p->wz &&
-                               !p->c_length && !p->theta && !p->phi && !p->area && !p->bond_scale &&
-                               !p->id && !p->cpu && !p->n_bnds && !p->seg_id1 && !p->seg_id2 && !p->site &&
-                               !p->position && !p->fuse_tip && !p->fix_site && !p->fuse_flag &&
-                               !p->split_flag && !p->new_flag && !p->dltd;
-    if (n && only_required && ctx->have_state && ctx->n == n && ctx->offsets == off && !ctx->S.has_rods) {
+    if (same_cand) {
         cudaStream_t st = ctx->stream;
-        if (int rc = sync_fp64(ctx)) return rc;
-        if (join.s) CK(cudaStreamWaitEvent(st, ctx->io_ev[1], 0));  // staged positions
+        const int grd = grid_for(ctx, ctx->sh_misc, n), blk = ctx->sh_misc.block;
+        const DevState &S = ctx->S;
         CK(cudaMemsetAsync(ctx->d_chk, 0, sizeof(unsigned long long), st));
-        LAUNCH(launch_same_state(ctx->S, ctx->parity, src_x, src_y, src_z, src_r, src_ct, ctx->d_chk,
-                                 grid_for(ctx, ctx->sh_misc, n), ctx->sh_misc.block, st));
+        if (join.s) {  // each field as its copy lands: only the last comparison follows the copies
+            LAUNCH(launch_same_state(S, ctx->parity, nullptr, nullptr, nullptr, src_r, src_ct, ctx->d_chk, grd, blk,
+                                     st));
+            CK(cudaStreamWaitEvent(st, ctx->io_ev[6], 0));
+            LAUNCH(launch_same_state(S, ctx->parity, src_x, nullptr, nullptr, nullptr, nullptr, ctx->d_chk, grd, blk,
+                                     st));
+            CK(cudaStreamWaitEvent(st, ctx->io_ev[7], 0));
+            LAUNCH(launch_same_state(S, ctx->parity, nullptr, src_y, nullptr, nullptr, nullptr, ctx->d_chk, grd, blk,
+                                     st));
+            CK(cudaStreamWaitEvent(st, ctx->io_ev[1], 0));
+            LAUNCH(launch_same_state(S, ctx->parity, nullptr, nullptr, src_z, nullptr, nullptr, ctx->d_chk, grd, blk,
+                                     st));
+        } else {
+            LAUNCH(launch_same_state(S, ctx->parity, src_x, src_y, src_z, src_r, src_ct, ctx->d_chk, grd, blk, st));
+        }
         CK(cudaMemcpyAsync(ctx->h_chk, ctx->d_chk, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         if (ctx->h_chk[0] == 0) {
-            DevState &S = ctx->S;
-            for (double *v : {S.vx, S.vy, S.vz, S.wx, S.wy, S.wz})
-                CK(cudaMemsetAsync(v, 0, sizeof(double) * n, st));
+            // velocities to zero (unless no kernel wrote them since the last
+            // load zeroed them) and the counters; stream-ordered before
+            // whatever the caller enqueues next
+            if (!ctx->vel64_zero)
+                for (double *v : {S.vx, S.vy, S.vz, S.wx, S.wy, S.wz})
+                    CK(cudaMemsetAsync(v, 0, sizeof(double) * n, st));
             CK(cudaMemsetAsync(ctx->d_cnt, 0, sizeof(DevCounters), st));
-            CK(cudaStreamSynchronize(st));
+            CK(cudaGetLastError());
+            ctx->vel64_zero = true;
             ctx->stepped = false;
             ctx->vel32 = false;
             ctx->pcap_valid = false;
@@ -598,6 +624,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
             return BMXG_OK;
         }
     }
+    ctx->vel64_zero = false;  // (until the full load below has set every plane)
     // cell types decide which path runs (rods need their fields) and the
     // largest radius whether the FP32F list is exact: checked on the device,
     // one small read-back
@@ -764,6 +791,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     ctx->have_state = true;
     ctx->stepped = false;
     ctx->vel32 = false;
+    ctx->vel64_zero = !p->velx && !p->vely && !p->velz && !p->wx && !p->wy && !p->wz;
     ctx->step_count = 0;
     ctx->parity = 0;
     ctx->rmax = rmax;
@@ -1206,6 +1234,7 @@ extern "C" {
 int bmxg_prepare(bmxg_ctx *ctx, double dt, int32_t precision)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (!std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt");
@@ -1227,6 +1256,8 @@ int bmxg_prepare(bmxg_ctx *ctx, double dt, int32_t precision)
 int bmxg_step(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t precision)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    // an FP32F sphere step writes the FP32 velocity planes only
+    if (precision != BMXG_FP32F || ctx->S.has_rods) ctx->vel64_zero = false;
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt or nsteps");
@@ -1362,6 +1393,7 @@ int bmxg_step_tile(bmxg_ctx *ctx, const bmxg_tile *tile, const bmxg_particles *r
                    double dt, int32_t where)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!tile || !reals || reals->n < 0 || (ghosts && ghosts->n < 0)) return fail(ctx, BMXG_ERR_ARG, "bad arguments");
     if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
@@ -1574,6 +1606,7 @@ int bmxg_particle_exchange(bmxg_ctx *ctx, const double *vol, double *conc, doubl
                            int32_t where)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (!vol || !conc || !xpar || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "vol, conc, xpar and a finite dt are required");
@@ -1626,6 +1659,7 @@ int bmxg_set_list_mode(bmxg_ctx *ctx, int32_t mode)
 int bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflow)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (added) *added = 0;
     if (overflow) *overflow = 0;
@@ -1658,6 +1692,7 @@ int bmxg_init_bonds(bmxg_ctx *ctx, double rlim, int64_t *added, int64_t *overflo
 int bmxg_autotune(bmxg_ctx *ctx, const char *cache_path)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (ctx->n == 0 || ctx->S.has_rods) return BMXG_OK;
@@ -1983,6 +2018,7 @@ extern "C" {
 int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
     if (ctx->S.has_rods) return fail(ctx, BMXG_ERR_UNSUPPORTED, "the differentiation form covers spheres");
     if (nsteps < 0 || ckpt_every < 1 || !std::isfinite(dt)) return fail(ctx, BMXG_ERR_ARG, "bad dt, nsteps or ckpt_every");
@@ -2029,6 +2065,7 @@ int bmxg_forward(bmxg_ctx *ctx, double dt, int32_t nsteps, int32_t ckpt_every)
 int bmxg_backward(bmxg_ctx *ctx, const double *dL_dx, double *dL_dx0, double *dL_dparams, double *dL_dadhesion)
 {
     if (!ctx) return BMXG_ERR_ARG;
+    ctx->vel64_zero = false;  // (its kernels may write the FP64 velocity planes)
     if (ctx->traj_T < 0) return fail(ctx, BMXG_ERR_STATE, "bmxg_forward must run first");
     if (!dL_dx) return fail(ctx, BMXG_ERR_ARG, "dL_dx is required");
     (void)cudaGetLastError();

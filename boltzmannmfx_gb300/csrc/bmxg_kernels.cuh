@@ -166,9 +166,11 @@ int launch_rebuild(const DevState &S, int b, int *scan_scratch, int grid, int bl
 int launch_load_slots(const DevState &S, const double *ux, const double *uy, const double *uz, const double *ur,
                       const int *uct, const int *ucol, const int *uiz, const int *uperm, int grid, int block,
                       cudaStream_t st);
-// state checks before a load: out[4] = {bad cell type, any FUNGI, largest radius bits, NaN radius}
+// *diff |= 1 when a given field (null: not compared) differs bit for bit from
+// the device state of buffer a (slot s against caller index orig[s])
 int launch_same_state(const DevState &S, int a, const double *x, const double *y, const double *z, const double *r,
                       const int *ct, unsigned long long *diff, int grid, int block, cudaStream_t st);
+// state checks before a load: out[4] = {bad cell type, any FUNGI, largest radius bits, NaN radius}
 int launch_check_state(const int *ct, const double *r, int n, unsigned long long *out, int grid, int block,
                        cudaStream_t st);
 

@@ -322,11 +322,12 @@ __global__ void k_same_state(const DevState S, int a, const double *__restrict__
             d = 1u;
             continue;
         }
-        d |= (__double_as_longlong(x[i]) != __double_as_longlong(S.x[a][s])) ? 1u : 0u;
-        d |= (__double_as_longlong(y[i]) != __double_as_longlong(S.y[a][s])) ? 1u : 0u;
-        d |= (__double_as_longlong(z[i]) != __double_as_longlong(S.z[a][s])) ? 1u : 0u;
-        d |= (__double_as_longlong(r[i]) != __double_as_longlong(S.rad[s])) ? 1u : 0u;
-        d |= (ct[i] != (int)S.ctype[s]) ? 1u : 0u;
+        // (a null field is not compared: a load compares each field as its copy lands)
+        if (x) d |= (__double_as_longlong(x[i]) != __double_as_longlong(S.x[a][s])) ? 1u : 0u;
+        if (y) d |= (__double_as_longlong(y[i]) != __double_as_longlong(S.y[a][s])) ? 1u : 0u;
+        if (z) d |= (__double_as_longlong(z[i]) != __double_as_longlong(S.z[a][s])) ? 1u : 0u;
+        if (r) d |= (__double_as_longlong(r[i]) != __double_as_longlong(S.rad[s])) ? 1u : 0u;
+        if (ct) d |= (ct[i] != (int)S.ctype[s]) ? 1u : 0u;
     }
     d = __reduce_or_sync(0xffffffffu, d);
     if ((threadIdx.x & 31) == 0 && d) atomicOr(diff, 1ull);

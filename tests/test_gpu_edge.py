@@ -258,3 +258,27 @@ def test_reloading_the_stored_state_keeps_the_trajectory(gpu_lib, precision):
     cd.get_state(D, fout)
     for k in fout:
         assert np.array_equal(C1[k], D[k]), k
+
+
+def test_reload_reads_zero_velocities_after_either_form(gpu_lib):
+    """A reload of the stored state resets the velocities whichever form
+    stepped before it: after an FP64 step (its velocity planes written) and
+    after FP32F steps (the FP64 planes left as the last load zeroed them)."""
+    w = configs.colonies(ncol=4, nmin=2_000, nmax=8_000)
+    fin = ("x", "y", "z", "radius", "cell_type")
+    fout = ("x", "y", "z", "velx", "vely", "velz")
+    B = w.particles.copy()
+    cb = Context(w.params, w.geoms)
+    cb.set_state(B, w.offsets, fields=fin)
+    for form in (BMXG_FP64, BMXG_FP32F, BMXG_FP32F, BMXG_FP64, BMXG_FP64, BMXG_FP32F):
+        cb.step(w.dt, 2, form)
+        cb.get_state(B, fout)
+        assert np.any(B["velz"])
+        cb.set_state(B, w.offsets, fields=fin)
+        Z = B.copy()
+        cb.get_state(Z, fout)
+        for k in ("velx", "vely", "velz"):
+            assert not np.any(Z[k]), (form, k)
+        for k in ("x", "y", "z"):
+            assert np.array_equal(Z[k], B[k]), (form, k)
+    cb.close()
