@@ -11,7 +11,8 @@ with the plain FP64 form on the same workload beside it.
          larger than L2, or L2 is flushed between steps for small workloads).
 `e2e`    the same metric through the C ABI with host buffers: every step
          copies x, y, z, radius, cell_type in (bmxg_set_state) and x, y, z,
-         vel out (bmxg_get_state) from pinned host memory.
+         vel out (bmxg_get_state) from pinned host memory; the median of
+         three host-timed windows of up to 20 calls.
 `roofline` the force kernel (the dominant one) timed per launch with CUDA
          events in profiling mode, against the algorithmic bytes per
          particle-step (64 B for the FP32 sphere form, 80 B for FP64 spheres)
@@ -612,31 +613,43 @@ def run_ours(args):
         ctx.set_state(H, w.offsets, fields=fin)
         ctx.step(w.dt, 1, prec)
         ctx.get_state(H, fout)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(ke):
-        ctx.set_state(H, w.offsets, fields=fin)
-        ctx.step(w.dt, 1, prec)
-        ctx.get_state(H, fout)
-    te = time.perf_counter() - t0
+    # three windows of ke calls, timed on the host clock; the median window
+    # is reported (one host stall in a window does not set the figure)
+    wins = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ctx.set_state(H, w.offsets, fields=fin)
+            ctx.step(w.dt, 1, prec)
+            ctx.get_state(H, fout)
+        wins.append(time.perf_counter() - t0)
+    te = float(np.median(wins))
     e2e = {"value": N * world * ke / te, "unit": UNIT,
            "h2d_bytes_per_step": int(H.nbytes(fin)), "d2h_bytes_per_step": int(H.nbytes(fout)),
-           "steps": ke, "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)",
-           "note": "a caller loading back the state it stored keeps the device's slot order and list"}
+           "steps": ke, "windows_ms_per_call": [round(1e3 * t / ke, 4) for t in wins],
+           "path": "bmxg_set_state + bmxg_step + bmxg_get_state (host buffers)",
+           "note": "a caller loading back the state it stored keeps the device's slot order and list; "
+                   "the median of three windows of `steps` calls"}
     # the same calls when every load differs from the stored state (as after
     # split_particles and ParticleExchange in bmx::Evolve): one particle moved
     # by one ulp each call, so each load re-sorts and the step runs the
     # per-step path
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for it in range(ke):
-        H["x"][it % N] = np.nextafter(H["x"][it % N], 1.0)
-        ctx.set_state(H, w.offsets, fields=fin)
-        ctx.step(w.dt, 1, prec)
-        ctx.get_state(H, fout)
-    tc = time.perf_counter() - t0
+    wins = []
+    for r in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for it in range(ke):
+            k = (r * ke + it) % N
+            H["x"][k] = np.nextafter(H["x"][k], 1.0)
+            ctx.set_state(H, w.offsets, fields=fin)
+            ctx.step(w.dt, 1, prec)
+            ctx.get_state(H, fout)
+        wins.append(time.perf_counter() - t0)
+    tc = float(np.median(wins))
     e2e_changed = {"value": N * world * ke / tc, "unit": UNIT, "steps": ke, "ms_per_call": 1e3 * tc / ke,
-                   "path": "the e2e calls with a changed state every call (full load)"}
+                   "windows_ms_per_call": [round(1e3 * t / ke, 4) for t in wins],
+                   "path": "the e2e calls with a changed state every call (full load); the median of three windows"}
 
     adj = None
     split = None
@@ -665,7 +678,8 @@ def run_ours(args):
                                     "steps": args.steps,
                                     "per_step": "k_list_decide + k_list_step",
                                     "per_build": "k_list_rebin, 3 scan kernels, k_list_scatter, k_list_canon, "
-                                                 "k_list_build, k_list_xcount, 3 scan kernels, k_list_xcopy "
+                                                 "k_list_cells, k_list_build, k_list_xcount, 3 scan kernels, "
+                                                 "k_list_xcopy "
                                                  "(CUDA-graph conditional node)"}
                                    if list_mode else
                                    {"kind": "per-step binning", "rebins": int(rebins), "steps": args.steps}),

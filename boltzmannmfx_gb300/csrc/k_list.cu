@@ -825,8 +825,8 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     int k = 1 + launch_scan(S.colcnt, S.colstart[kListBins], S.ncols_total, scan_scratch, st, gate);
     k_list_scatter<<<g1, block, 0, st>>>(S);
     k_list_canon<<<g1, block, 0, st>>>(S, a);
-    // the cell offsets: up to 64 blocks of columns per colony
-    const dim3 gc(S.ncol, std::max(1, std::min(64, (S.cols_max + kCellsBlock - 1) / kCellsBlock)));
+    // the cell offsets: a block per kCellsBlock columns of the largest colony
+    const dim3 gc(S.ncol, std::max(1, std::min(65535, (S.cols_max + kCellsBlock - 1) / kCellsBlock)));
     k_list_cells<<<gc, kCellsBlock, 0, st>>>(S);
     // the build: one slot per thread in small blocks (the stencil walks
     // differ in length from slot to slot; small blocks on a grid of every
