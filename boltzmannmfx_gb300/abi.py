@@ -189,9 +189,18 @@ class Particles:
         return q
 
     def struct(self, fields=None):
+        # the struct of the last call with the same fields, while it still
+        # points at this container's arrays (a load-step-store loop builds it
+        # once instead of every call)
+        key = None if fields is None else tuple(fields)
+        cache = self.__dict__.setdefault("_structs", {})
+        hit = cache.get(key)
+        if hit is not None and hit[0].n == self.n and all(self.a[k] is v for k, v in hit[1]):
+            return hit[0]
         s = ParticlesStruct()
         s.n = self.n
         want = set(fields) if fields is not None else None
+        used = []
         for name, ctype in ParticlesStruct._fields_[1:]:
             if want is not None and name not in want:
                 setattr(s, name, ctype())
@@ -199,6 +208,8 @@ class Particles:
             arr = self.a[name]
             assert arr.flags["C_CONTIGUOUS"]
             setattr(s, name, arr.ctypes.data_as(ctype))
+            used.append((name, arr))
+        cache[key] = (s, tuple(used))
         return s
 
     def nbytes(self, fields):

@@ -156,8 +156,12 @@ class Context:
         s = P.struct(fields)
         off = None
         if offsets is not None and len(self.geoms) > 1:
-            self._off = np.ascontiguousarray(offsets, np.int64)
-            off = self._off.ctypes.data_as(C.POINTER(C.c_int64))
+            # (the same offsets array as the last call: its int64 copy and pointer are kept)
+            if getattr(self, "_off_src", None) is not offsets or not np.array_equal(self._off, offsets):
+                self._off = np.array(offsets, np.int64)
+                self._off_ptr = self._off.ctypes.data_as(C.POINTER(C.c_int64))
+                self._off_src = offsets
+            off = self._off_ptr
         self._check(self.lib.bmxg_set_state(self.h, C.byref(s), off, where))
         self.n = P.n
 
