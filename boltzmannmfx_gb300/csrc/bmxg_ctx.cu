@@ -811,9 +811,14 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     if (!ctx) return BMXG_ERR_ARG;
     (void)cudaGetLastError();  // drop a non-sticky error another library left on this thread
     if (!ctx->have_state) return fail(ctx, BMXG_ERR_STATE, "no state loaded");
-    if (int rc = sync_fp64(ctx)) return rc;
     if (!p || p->n != ctx->n) return fail(ctx, BMXG_ERR_ARG, "particle count differs from the loaded state");
     if (where != BMXG_HOST && where != BMXG_DEVICE) return fail(ctx, BMXG_ERR_ARG, "bad `where`");
+    // positions still in the list's fixed point: host arrays asking for x, y
+    // and z get each axis converted as it is stored (one pass instead of a
+    // conversion and a scatter); otherwise all three are converted first
+    const bool fx_store = ctx->fx_ahead && where == BMXG_HOST && p->x && p->y && p->z;
+    if (!fx_store)
+        if (int rc = sync_fp64(ctx)) return rc;
     const int64_t n = ctx->n;
     if (n == 0) return BMXG_OK;
     const DevState &S = ctx->S;
@@ -880,9 +885,19 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
         return finish(dst, sizeof(double) * n);
     };
     int rc;
-    if ((rc = out_d(p->x, S.x[a]))) return rc;
-    if ((rc = out_d(p->y, S.y[a]))) return rc;
-    if ((rc = out_d(p->z, S.z[a]))) return rc;
+    if (fx_store) {
+        double *dst[3] = {p->x, p->y, p->z};
+        for (int ax = 0; ax < 3; ++ax) {
+            double *o = (double *)begin(dst[ax]);
+            LAUNCH(launch_list_to_fp64_axis(S, a, ax, o, blk, st));
+            if ((rc = finish(dst[ax], sizeof(double) * n))) return rc;
+        }
+        ctx->fx_ahead = false;
+    } else {
+        if ((rc = out_d(p->x, S.x[a]))) return rc;
+        if ((rc = out_d(p->y, S.y[a]))) return rc;
+        if ((rc = out_d(p->z, S.z[a]))) return rc;
+    }
     if (ctx->vel32) {
         if ((rc = out_f(p->velx, S.vxf))) return rc;
         if ((rc = out_f(p->vely, S.vyf))) return rc;

@@ -207,6 +207,8 @@ int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond,
 // list starts on a state), and back (whenever the FP64 positions are read)
 int launch_list_init(const DevState &S, int a, int grid, int block, cudaStream_t st);
 int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStream_t st);
+// axis ax (0 x, 1 y, 2 z) of it, also scattered to out in the caller's order (out[orig[i]])
+int launch_list_to_fp64_axis(const DevState &S, int a, int ax, double *out, int block, cudaStream_t st);
 // rebuild (gated on lctl->rebuild): bins of buffer a's positions into the
 // list bins, column lists, and the list itself
 // (returns the kernels it enqueues, kListBodyKernels)

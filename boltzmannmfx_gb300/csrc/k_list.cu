@@ -787,6 +787,24 @@ __global__ void k_list_to_fp64(const DevState S, int a)
     }
 }
 
+// One axis of the same conversion, the value also scattered to the caller's
+// order (out[orig[i]]): a store of the state converts and gathers in one pass.
+__global__ void k_list_to_fp64_axis(const DevState S, int a, int ax, double *out)
+{
+    const int n = S.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int col = block_colony(S, i);
+    if (i < n) {
+        const FxGeom &F = S.fxg[col];
+        const int4 h = S.fxh[a][i];
+        const unsigned hi = (unsigned)(ax == 0 ? h.x : (ax == 1 ? h.y : h.z));
+        const double v = from_fx(fx_join(hi, S.fxl[a][(size_t)ax * n + i]), F, ax);
+        (ax == 0 ? S.x : (ax == 1 ? S.y : S.z))[a][i] = v;
+        const int o = S.orig[i];
+        if ((unsigned)o < (unsigned)n) out[o] = v;
+    }
+}
+
 }  // namespace
 
 int launch_list_decide(const DevState &S, unsigned long long cond, int use_cond, cudaStream_t st)
@@ -806,6 +824,12 @@ int launch_list_to_fp64(const DevState &S, int a, int grid, int block, cudaStrea
 {
     (void)grid;  // one slot per thread
     k_list_to_fp64<<<(S.n + block - 1) / block, block, 0, st>>>(S, a);
+    return 1;
+}
+
+int launch_list_to_fp64_axis(const DevState &S, int a, int ax, double *out, int block, cudaStream_t st)
+{
+    k_list_to_fp64_axis<<<(S.n + block - 1) / block, block, 0, st>>>(S, a, ax, out);
     return 1;
 }
 
