@@ -683,7 +683,7 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
         AL(S.perm[k], n); AL(S.colstart[k], ncols + 1);
         AL(S.srel[k], n); AL(S.siz[k], n); AL(S.rank[k], n);
     }
-    AL(S.colcnt, ncols); AL(S.tmp, n);
+    AL(S.colcnt, ncols); AL(S.tmp, n); AL(S.lkey, n);
     AL(S.rad, n); AL(S.orig, n); AL(S.ctype, n);
     AL(S.vx, n); AL(S.vy, n); AL(S.vz, n); AL(S.wx, n); AL(S.wy, n); AL(S.wz, n);
     AL(S.vxf, n); AL(S.vyf, n); AL(S.vzf, n);
@@ -1004,7 +1004,6 @@ int ensure_list(bmxg_ctx *ctx, float skin)
             if ((rc = dalloc(ctx, &S.fxh[k], ctx->n))) return rc;
             if ((rc = dalloc(ctx, &S.fxl[k], 3 * (size_t)ctx->n))) return rc;
         }
-        if ((rc = dalloc(ctx, &S.lkey, ctx->n))) return rc;
         if ((rc = dalloc(ctx, &S.cellstart, ctx->ncells_total + 1))) return rc;
         // (the scratch serves the scan of the column counts and that of the groups' entries)
         const int nscan = (int)std::max<int64_t>(S.ncols_total, ((int64_t)ctx->n + 31) / 32);

@@ -135,8 +135,9 @@ struct DevState {
     const FxGeom *fxg; // per colony
     int *pcap;         // null, or per slot 1 + kPairCap ints: the gated pairs of the last
                        // list step (count, then neighbour slots in accumulation order)
-    unsigned long long *lkey;  // build scratch, n: at each column position the counting sort
-                               // gave a slot, that slot's (z bin, caller index) key
+    unsigned long long *lkey;  // sort scratch, n (the load's sort and the list build): at each
+                               // column position the counting sort gave a particle, its
+                               // (z bin, caller index) key
     int *cellstart;    // ncells_total + 1 offsets of the cells in the sorted copies
     int ncells_total;
     int cols_max;      // largest column count of a colony
@@ -177,6 +178,7 @@ int launch_check_state(const int *ct, const double *r, int n, unsigned long long
 // caller-order staging -> slot order (set_state) and back (get_state)
 int launch_user_bin(const DevState &S, const double *ux, const double *uy, const double *uz,
                      int *ucol, int *uiz, int grid, int block, cudaStream_t st);
+// the caller's particles into column order: uperm[slot] = caller index (keys in lkey)
 int launch_user_scatter_canon(const DevState &S, const int *ucol, const int *uiz, const int *colstart,
                                int *uperm, int grid, int block, cudaStream_t st);
 int launch_gather_d(double *dst, const double *src, const int *perm, int n, int grid, int block, cudaStream_t st);

@@ -200,30 +200,16 @@ __global__ void k_user_bin(const DevState S, const double *ux, const double *uy,
     }
 }
 
-__global__ void k_user_scatter(const DevState S, const int *ucol, const int *colstart)
+// counting sort of the caller's particles into the columns (arrival order
+// from the atomics): each particle's (z bin, caller index) key at the
+// position it drew
+__global__ void k_user_scatter(const DevState S, const int *ucol, const int *uiz, const int *colstart)
 {
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
         const int c = ucol[u];
         const int r = atomicSub(&S.colcnt[c], 1) - 1;
         const int t = colstart[c] + r;
-        if (t >= 0 && t < S.n) S.tmp[t] = u;
-        else atomicAdd(&S.cnt->bad_index, 1ULL);
-    }
-}
-
-__global__ void k_user_canon(const DevState S, const int *ucol, const int *uiz, const int *colstart,
-                             int *uperm)
-{
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
-        const int c = ucol[u];
-        const int s0 = max(colstart[c], 0), s1 = min(colstart[c + 1], S.n);
-        const unsigned long long key = col_key(uiz[u], u);
-        int rank = 0;
-        for (int t = s0; t < s1; ++t) {
-            const int v = S.tmp[t];
-            if ((unsigned)v < (unsigned)S.n) rank += (col_key(uiz[v], v) < key);
-        }
-        if (s0 + rank < s1) uperm[s0 + rank] = u;
+        if (t >= 0 && t < S.n) S.lkey[t] = col_key(uiz[u], u);
         else atomicAdd(&S.cnt->bad_index, 1ULL);
     }
 }
@@ -359,6 +345,21 @@ __global__ void k_check_state(const int *__restrict__ ct, const double *__restri
     }
 }
 
+// Caller particle u's slot: its column's start + its rank among the
+// column's keys (z bin, then caller index): uperm[slot] = u.
+__global__ void k_user_canon(const DevState S, const int *ucol, const int *uiz, const int *colstart, int *uperm)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < S.n; u += gridDim.x * blockDim.x) {
+        const int c = ucol[u];
+        const int s0 = max(colstart[c], 0), s1 = min(colstart[c + 1], S.n);
+        const unsigned long long key = col_key(uiz[u], u);
+        int rank = 0;
+        for (int t = s0; t < s1; ++t) rank += (__ldg(&S.lkey[t]) < key);
+        if (s0 + rank < s1) uperm[s0 + rank] = u;
+        else atomicAdd(&S.cnt->bad_index, 1ULL);
+    }
+}
+
 // Slot s of a freshly sorted state holds caller particle uperm[s]: its
 // position, radius and cell type are gathered from the caller-order arrays,
 // its bins are the caller-order bins of the sort, its column order is the
@@ -462,7 +463,7 @@ int launch_user_bin(const DevState &S, const double *ux, const double *uy, const
 int launch_user_scatter_canon(const DevState &S, const int *ucol, const int *uiz, const int *colstart,
                                int *uperm, int grid, int block, cudaStream_t st)
 {
-    k_user_scatter<<<grid, block, 0, st>>>(S, ucol, colstart);
+    k_user_scatter<<<grid, block, 0, st>>>(S, ucol, uiz, colstart);
     k_user_canon<<<grid, block, 0, st>>>(S, ucol, uiz, colstart, uperm);
     return 2;
 }
