@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from boltzmannmfx_gb300 import Context, configs
-from boltzmannmfx_gb300.abi import BMXG_FP32F
+from boltzmannmfx_gb300.abi import BMXG_FP32F, Particles
 from common import relerr
 
 pytestmark = pytest.mark.gpu
@@ -45,6 +45,61 @@ def gated_pairs(O, prm, g, P):
     return i, idx, r, rlm, keep
 
 
+def compare_gated(O, prm, geoms, offsets, Q, offs, idx, colonies):
+    """The step's gated pairs of the given colonies against the reference's:
+    equal outside the FP32 band, none twice; returns (pairs, pairs in the band)."""
+    total = band = 0
+    for c in colonies:
+        lo, hi = int(offsets[c]), int(offsets[c + 1])
+        P = Q.subset(lo, hi)
+        i, j, r, rlm, keep = gated_pairs(O, prm, geoms[c], P)
+        ref = {}
+        for a, b, k in zip(i.tolist(), j.tolist(), keep.tolist()):
+            if k:
+                ref.setdefault(a, []).append(b)
+        near = {(a, b) for a, b, rr, rl in zip(i.tolist(), j.tolist(), r.tolist(), rlm.tolist())
+                if abs(rr - rl) <= BAND * rl}
+        for a in range(P.n):
+            got = set((idx[offs[lo + a]:offs[lo + a + 1]] - lo).tolist())
+            want = set(ref.get(a, []))
+            assert len(got) == offs[lo + a + 1] - offs[lo + a], "a pair accumulated twice"
+            diff = got ^ want
+            for b in diff:
+                assert (a, b) in near, (c, a, b)
+            band += len(diff)
+            total += len(want)
+    return total, band
+
+
+def test_list_cells_of_tall_short_and_narrow_boxes(gpu_lib, oracle_lib):
+    """Colonies in boxes 28, 45, 70 and 32 z bins tall and of unequal x-y
+    extents (the list build writes each column's cell offsets 32 z bins at a
+    time): after list steps with builds, the step's gated pairs equal the
+    reference's per colony."""
+    rng = np.random.default_rng(11)
+    specs = [(0.128, 0.128, 0.056, 6000), (0.064, 0.128, 0.090, 5000), (0.128, 0.064, 0.140, 7000),
+             (0.096, 0.096, 0.064, 3000)]
+    parts = [configs.sphere_colony(k, lx, ly, rng) for lx, ly, lz, k in specs]
+    geoms = [configs.box_geometry(lx, ly, lz) for lx, ly, lz, k in specs]
+    assert [g.n_cell[2] for g in geoms] == [28, 45, 70, 32]
+    P = Particles.concat(parts)
+    off = np.concatenate([[0], np.cumsum([p.n for p in parts])]).astype(np.int64)
+    prm = configs.deck_params()
+    ctx = Context(prm, geoms)
+    ctx.set_state(P, off)
+    ctx.step(0.25, 40, BMXG_FP32F)
+    assert 2 <= ctx.stats()["n_rebins"] < 40
+    Q = P.copy()
+    ctx.get_state(Q, ("x", "y", "z"))
+    ctx.set_pair_capture(True)
+    ctx.step(0.25, 1, BMXG_FP32F)
+    offs, idx = ctx.step_pairs()
+    ctx.close()
+    total, band = compare_gated(oracle_lib, prm, geoms, off, Q, offs, idx, range(len(specs)))
+    assert total > 10_000
+    assert band <= 1e-4 * total, (band, total)
+
+
 def test_list_step_gated_pairs_and_forces_on_the_colonies(gpu_lib, oracle_lib):
     w = configs.colonies()
     ctx = Context(w.params, w.geoms)
@@ -62,29 +117,12 @@ def test_list_step_gated_pairs_and_forces_on_the_colonies(gpu_lib, oracle_lib):
     sizes = np.diff(w.offsets)
     order = np.argsort(sizes)
     sample = sorted(set(order[::16].tolist()) | {int(order[-1]), int(order[0])})
-    total = band = 0
+    total, band = compare_gated(oracle_lib, w.params, w.geoms, w.offsets, Q, offs, idx, sample)
     for c in sample:
-        lo, hi = int(w.offsets[c]), int(w.offsets[c + 1])
-        P = Q.subset(lo, hi)
-        g = w.geoms[c]
-        i, j, r, rlm, keep = gated_pairs(oracle_lib, w.params, g, P)
-        ref = {}
-        for a, b, k in zip(i.tolist(), j.tolist(), keep.tolist()):
-            if k:
-                ref.setdefault(a, []).append(b)
-        near = {(a, b) for a, b, rr, rl in zip(i.tolist(), j.tolist(), r.tolist(), rlm.tolist())
-                if abs(rr - rl) <= BAND * rl}
-        for a in range(P.n):
-            got = set((idx[offs[lo + a]:offs[lo + a + 1]] - lo).tolist())
-            want = set(ref.get(a, []))
-            assert len(got) == offs[lo + a + 1] - offs[lo + a], "a pair accumulated twice"
-            diff = got ^ want
-            for b in diff:
-                assert (a, b) in near, (c, a, b)
-            band += len(diff)
-            total += len(want)
         # the step's force on these positions against the FP64 oracle
-        Pr = P.copy()
+        lo, hi = int(w.offsets[c]), int(w.offsets[c + 1])
+        g = w.geoms[c]
+        Pr = Q.subset(lo, hi)
         fc = oracle_lib.forces(w.params, g, Pr, oracle_lib.pairs(w.params, g, Pr), nthreads=8)
         got_v = np.stack([V["velx"][lo:hi], V["vely"][lo:hi], V["velz"][lo:hi]])
         assert relerr(got_v, fc[:3]) <= TOL32, c
