@@ -301,9 +301,9 @@ __global__ void __launch_bounds__(kCellsBlock) k_list_cells(const DevState S)
 // Visit the slots of the 3 x 3 neighbour columns of bin (bx, by), z bins
 // izi - 1 .. izi + 1 (periodic images included), as contiguous cell ranges
 // of the sorted copies: f(u) for each sorted position u but the slot's own
-// self_t.  Order: x rows outermost, then y, then z, ascending caller index
-// within a cell.
-template <class F>
+// self_t (SKIP_SELF; otherwise f sees it too and excludes it itself).  Order:
+// x rows outermost, then y, then z, ascending caller index within a cell.
+template <bool SKIP_SELF = true, class F>
 __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G, int self_t, int bx, int by, int izi,
                                             F &&f)
 {
@@ -325,7 +325,7 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
             const int cb = G.cell_base + ((sx - 1) * G.n[1] + (sy - 1)) * nz;
             const int hi = __ldg(&cs[cb + z1]);
             for (int u = __ldg(&cs[cb + z0 - 1]); u < hi; ++u) {
-                if (u == self_t) continue;
+                if (SKIP_SELF && u == self_t) continue;
                 f(u);
             }
         }
@@ -335,7 +335,10 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
 // List build: every slot (in sorted order, so a warp's lanes share cells)
 // keeps the neighbours closer than rA + skin on the exact fixed-point
 // differences of the high words (+ a slack of four units per component and
-// the FP32 rounding of the test), and its list length.
+// the FP32 rounding of the test), and its list length.  The rounding margin:
+// the offsets' unit factors are scaled by 1 - 1e-6 (r^2 by 1 - 2e-6), against
+// at most ~4e-7 of relative FP32 rounding in r^2 and in the bound squared;
+// the slot's own record passes the test (distance 0) and is dropped after it.
 __global__ void __launch_bounds__(256, 6) k_list_build(const DevState S, const DevParams P)
 {
     if (!S.lctl->rebuild) return;
@@ -354,19 +357,19 @@ __global__ void __launch_bounds__(256, 6) k_list_build(const DevState S, const D
         col_to_bxy(G, S.col[B][i], bx, by);
         const int izi = S.siz[B][t];
         const int4 me = sg[t];
-        const float ux = F.uh[0], uy = F.uh[1], uz = F.uh[2];
         const float ri = __int_as_float(me.w);
-        const float lim0 = reach + 4.0f * (ux + uy + uz);
+        const float ci = ri + (reach + 4.0f * (F.uh[0] + F.uh[1] + F.uh[2]));  // the bound less r_j
+        const float ux = F.uh[0] * 0.999999f, uy = F.uh[1] * 0.999999f, uz = F.uh[2] * 0.999999f;
         int c = 0;
         int4 rec = make_int4(0, 0, 0, 0);
-        visit_cells(S, G, t, bx, by, izi, [&](int s) {
+        visit_cells<false>(S, G, t, bx, by, izi, [&](int s) {
             const int4 q = __ldg(&sg[s]);
             const float ex = (float)(me.x - q.x) * ux;
             const float ey = (float)(me.y - q.y) * uy;
             const float ez = (float)(me.z - q.z) * uz;
             const float r2f = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
-            const float lim = ((ri + __int_as_float(q.w)) + lim0) * 1.000001f;
-            if (!(r2f <= lim * lim)) return;
+            const float lim = __int_as_float(q.w) + ci;
+            if (!(r2f <= lim * lim) || s == t) return;
             const int e = __ldg(&S.perm[B][s]);
             if (c == 0) rec.y = e;
             else if (c == 1) rec.z = e;
