@@ -112,7 +112,7 @@ struct bmxg_ctx {
     bool bins_exact = true;       // bins of buffer `parity` are the reference's (list steps freeze them)
     double rmax = 0.0;            // largest radius of the state
     int64_t ncells_total = 0;     // 3D cells over all colonies
-    int *cell_scratch = nullptr;  // scan scratch of the cell counts
+    int *cell_scratch = nullptr;  // scan scratch of the list build (column counts, group entries)
     float skin_cur = 0.0f;        // skin of the list control block
     ListCtl *h_lctl = nullptr;    // pinned copy of the control block
     unsigned long long body_runs_seen = 0;  // list builds already counted as launches

@@ -31,10 +31,10 @@
 // build launches two kernels.
 //
 // Build: bins from the high words (integer arithmetic, consistent with the
-// positions), a counting sort into 3D cells, the in-cell order by caller
-// index (deterministic lists and FP32 summation order), and the stencil walk
-// that keeps every candidate within rA + skin on exact fixed-point
-// differences.
+// positions), a counting sort into the x-y columns, the in-column order by z
+// bin and caller index (deterministic lists and FP32 summation order), the 3D
+// cells' offsets from the sorted z bins, and the stencil walk that keeps
+// every candidate within rA + skin on exact fixed-point differences.
 //
 // Roofline: the step kernel streams 28 bytes of position state in and out,
 // the list in and the FP32 velocity out; the neighbour records it gathers
