@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) k_sphere64(const DevState S, const DevPar
 }
 
 template <bool SORTED>
-__global__ void __launch_bounds__(256) k_sphere32(const DevState S, const DevParams P, float dtf, int a,
+__global__ void __launch_bounds__(256, 5) k_sphere32(const DevState S, const DevParams P, float dtf, int a,
                                                   int resync)
 {
     const int b = a ^ 1;
