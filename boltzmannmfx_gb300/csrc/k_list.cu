@@ -136,11 +136,6 @@ __global__ void k_list_decide(ListCtl *c, DevCounters *cnt, cudaGraphConditional
     if (use_h) cudaGraphSetConditional(h, rb ? 1u : 0u);
 }
 
-__device__ __forceinline__ int cell_of(const DevGeom &G, int bx, int by, int bz)
-{
-    return G.cell_base + ((bx - 1) * G.n[1] + (by - 1)) * G.n[2] + (bz - 1);
-}
-
 // Colony of index i for a kernel whose blocks take consecutive indices, one
 // per thread: one binary search per block (the colonies of a block's range
 // are few), then each thread steps forward.  Slot order and the list's sorted
