@@ -145,6 +145,10 @@ __global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__res
 // Arrival order from the atomics is arbitrary; k_canon ranks every slot by
 // its (z bin, original index) key among the members of its column, which is
 // the order AMReX's serial binning gives (ascending index within a bin).
+// With key scratch (S.lkey: a context's state) the scatter leaves each slot's
+// key at the position it drew and the rank is counted over the column's keys;
+// without it (a bare caller's scratch) the slot index goes there and the
+// rank gathers each member's key.
 __global__ void k_scatter(const DevState S, int b, const int *gate)
 {
     if (gate && !*gate) return;
@@ -152,8 +156,12 @@ __global__ void k_scatter(const DevState S, int b, const int *gate)
         const int c = S.col[b][i];
         const int r = atomicSub(&S.colcnt[c], 1) - 1;  // leaves colcnt at zero
         const int t = S.colstart[b][c] + r;
-        if (t >= 0 && t < S.n) S.tmp[t] = i;
-        else atomicAdd(&S.cnt->bad_index, 1ULL);
+        if (t >= 0 && t < S.n) {
+            if (S.lkey) S.lkey[t] = col_key(S.iz[b][i], S.orig[i]);
+            else S.tmp[t] = i;
+        } else {
+            atomicAdd(&S.cnt->bad_index, 1ULL);
+        }
     }
 }
 
@@ -166,9 +174,13 @@ __global__ void k_canon(const DevState S, int b, int ra, const int *gate)
         const int izi = S.iz[b][i];
         const unsigned long long key = col_key(izi, S.orig[i]);
         int rank = 0;
-        for (int t = s0; t < s1; ++t) {
-            const int j = S.tmp[t];
-            if ((unsigned)j < (unsigned)S.n) rank += (col_key(S.iz[b][j], S.orig[j]) < key);
+        if (S.lkey) {
+            for (int t = s0; t < s1; ++t) rank += (__ldg(&S.lkey[t]) < key);
+        } else {
+            for (int t = s0; t < s1; ++t) {
+                const int j = S.tmp[t];
+                if ((unsigned)j < (unsigned)S.n) rank += (col_key(S.iz[b][j], S.orig[j]) < key);
+            }
         }
         const int t = s0 + rank;
         if (t >= s1) {  // i is not among its column's members: inconsistent counts
