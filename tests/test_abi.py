@@ -94,3 +94,28 @@ def test_no_cpu_fallback_in_product():
                 for pat in (r"^\s*(from|import)\s+oracle", r"liboracle", r"bmx_oracle", r"libbmxref",
                             r"orc_[a-z_]+\s*\("):
                     assert not re.search(pat, txt, re.M), (f, pat)
+
+
+def test_particles_struct_is_kept_while_its_arrays_are():
+    """Particles.struct: the same ctypes struct for the same fields while the
+    container's arrays are the same objects (a load-step-store loop builds it
+    once); a replaced array gives a new struct pointing at it; every pointer
+    is the array's own, and fields not asked for are null."""
+    import numpy as np
+    P = abi.Particles(100)
+    fin = ("x", "y", "z", "radius", "cell_type")
+    s1 = P.struct(fin)
+    assert P.struct(fin) is s1
+    assert P.struct(("x", "y")) is not s1
+    for k in fin:
+        assert C.cast(getattr(s1, k), C.c_void_p).value == P[k].ctypes.data, k
+    assert not getattr(s1, "velx")
+    P["x"] = np.arange(100.0)              # written in place: the same array
+    assert P.struct(fin) is s1
+    P.a["x"] = np.zeros(100)               # a new array object
+    s2 = P.struct(fin)
+    assert s2 is not s1
+    assert C.cast(s2.x, C.c_void_p).value == P["x"].ctypes.data
+    Q = P.copy()                           # a copy has its own arrays and structs
+    assert C.cast(Q.struct(fin).x, C.c_void_p).value == Q["x"].ctypes.data
+    assert Q.struct(fin).n == P.n
