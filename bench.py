@@ -678,7 +678,7 @@ def run_ours(args):
                                     "steps": args.steps,
                                     "per_step": "k_list_decide + k_list_step",
                                     "per_build": "k_list_rebin, 3 scan kernels, k_list_scatter, k_list_canon, "
-                                                 "k_list_cells, k_list_build, k_list_xcount, 3 scan kernels, "
+                                                 "k_list_cells, k_list_build, 3 scan kernels, "
                                                  "k_list_xcopy "
                                                  "(CUDA-graph conditional node)"}
                                    if list_mode else

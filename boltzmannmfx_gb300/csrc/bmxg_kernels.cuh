@@ -218,7 +218,7 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
                         int build_block, cudaStream_t st);
 // the list build kernel alone (gated on lctl->rebuild), build_block threads per block
 int launch_list_build(const DevState &S, const DevParams &P, int build_block, cudaStream_t st);
-constexpr int kListBodyKernels = 13;
+constexpr int kListBodyKernels = 12;
 // force + wall + update over the list, reading buffer a and writing buffer b
 // (grid = the SM count; passes of the block per chunk of slots, <= 0: a rule;
 // persistent: one wave of blocks taking chunks from a counter, else one block

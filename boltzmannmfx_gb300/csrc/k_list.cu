@@ -233,6 +233,7 @@ __global__ void k_list_canon(const DevState S, int a)
             S.siz[B][t] = bz;
             S.rank[B][i] = t;
         }
+        if ((i & 31) == 0) S.xcnt[i >> 5] = 0;  // the build adds up each group's entries
     }
 }
 
@@ -327,6 +328,13 @@ __device__ __forceinline__ void visit_cells(const DevState &S, const DevGeom &G,
     }
 }
 
+// Entries of slot i's list past the inline ones that the step takes from
+// the compacted list (none for a slot whose list overflowed: it walks).
+__device__ __forceinline__ int list_extra(int cnt)
+{
+    return (cnt > kNbrInline && cnt <= kNbrCap) ? cnt - kNbrInline : 0;
+}
+
 // List build: every slot (in sorted order, so a warp's lanes share cells)
 // keeps the neighbours closer than rA + skin on the exact fixed-point
 // differences of the high words (+ a slack of four units per component and
@@ -375,6 +383,8 @@ __global__ void __launch_bounds__(256, 6) k_list_build(const DevState S, const D
         rec.x = min(c, 255);
         S.lrec[i] = rec;
         if (c > kNbrCap) ++over;
+        const int x = list_extra(rec.x);  // its group's count of entries past the inline ones
+        if (x) atomicAdd(&S.xcnt[i >> 5], x);
     }
     if (over) atomicAdd(&S.lctl->overflow, over);
 }
@@ -395,26 +405,12 @@ struct PairRec {
     }
 };
 
-// Entries of slot i's list past the inline ones that the step takes from
-// the compacted list (none for a slot whose list overflowed: it walks).
-__device__ __forceinline__ int list_extra(int cnt)
-{
-    return (cnt > kNbrInline && cnt <= kNbrCap) ? cnt - kNbrInline : 0;
-}
-
 // Compaction of the list entries past the inline ones, per group of 32
-// consecutive slots (the step's warps): the groups' counts, then (after
-// their exclusive scan into xoff) each slot's entries copied from the
-// build's planes to xlist[xoff[group] + the entries of the group's earlier
-// slots].  One slot per thread, whole warps.
-__global__ void k_list_xcount(const DevState S)
-{
-    if (!S.lctl->rebuild) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int x = (i < S.n) ? list_extra(__ldg(&S.lrec[i].x) & 0xff) : 0;
-    const int t = __reduce_add_sync(0xffffffffu, x);
-    if ((threadIdx.x & 31) == 0 && i < S.n) S.xcnt[i >> 5] = t;
-}
+// consecutive slots (the step's warps): the groups' counts (added up by
+// k_list_build into counts that k_list_canon zeroed), then (after their
+// exclusive scan into xoff) each slot's entries copied from the build's
+// planes to xlist[xoff[group] + the entries of the group's earlier slots].
+// One slot per thread, whole warps.
 
 __global__ void k_list_xcopy(const DevState S)
 {
@@ -856,10 +852,9 @@ int launch_list_rebuild(const DevState &S, const DevParams &P, int a, int *scan_
     launch_list_build(S, P, build_block, st);
     // the entries past the inline ones, compacted per group of 32 slots
     const int gx = (S.n + 127) / 128;
-    k_list_xcount<<<gx, 128, 0, st>>>(S);
     k = k + launch_scan(S.xcnt, S.xoff, (S.n + 31) / 32, scan_scratch, st, gate);
     k_list_xcopy<<<gx, 128, 0, st>>>(S);
-    return k + 6;
+    return k + 5;
 }
 
 int launch_list_step(const DevState &S, const DevParams &P, double dt, int a, int grid, int block, int passes,

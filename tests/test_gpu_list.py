@@ -96,9 +96,9 @@ def test_graph_and_eager_steps_agree(gpu_lib):
     sa = A.stats()
     B.step(w.dt, 24, BMXG_FP32F)
     sb = B.stats()
-    # two kernels per step, thirteen per build, and the list's set-up (the
+    # two kernels per step, twelve per build, and the list's set-up (the
     # fixed-point positions) once
-    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 13 * sa["n_rebins"] + 1
+    assert sa["n_kernel_launches"] - l0 == 2 * 24 + 12 * sa["n_rebins"] + 1
     assert sa["n_rebins"] == sb["n_rebins"]
     QA, QB = read(A, w.particles), read(B, w.particles)
     for k in ("x", "y", "z", "velx", "vely", "velz"):
