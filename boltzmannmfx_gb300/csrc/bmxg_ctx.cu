@@ -550,8 +550,9 @@ int bmxg_set_state(bmxg_ctx *ctx, const bmxg_particles *p, const int64_t *colony
     const bool same_cand = n && only_required && ctx->have_state && ctx->n == n && ctx->offsets == off &&
                            !ctx->S.has_rods;
     // the comparison reads the device's FP64 positions
-    if (same_cand)
+    if (same_cand) {
         if (int rc = sync_fp64(ctx)) return rc;
+    }
     // Positions, radii and cell types: read in place from device arrays; host
     // arrays go to the staging, radii and cell types first on the compute
     // stream (the state checks need them), positions on the copy stream, so
@@ -817,8 +818,9 @@ int bmxg_get_state(bmxg_ctx *ctx, bmxg_particles *p, int where)
     // and z get each axis converted as it is stored (one pass instead of a
     // conversion and a scatter); otherwise all three are converted first
     const bool fx_store = ctx->fx_ahead && where == BMXG_HOST && p->x && p->y && p->z;
-    if (!fx_store)
+    if (!fx_store) {
         if (int rc = sync_fp64(ctx)) return rc;
+    }
     const int64_t n = ctx->n;
     if (n == 0) return BMXG_OK;
     const DevState &S = ctx->S;
